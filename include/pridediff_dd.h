@@ -1,0 +1,140 @@
+/*
+ * pridediff_dd.h -- C ABI of the GB300 distance-driven (DD) CT projector.
+ *
+ * Drop-in replacement for the operators of deeprecon's torch extension
+ * `radontorch` (deeprecon/interface/RadonTorch.cpp:1375-1418), exposed as a
+ * plain C ABI: device pointers, sizes, a host-side geometry record and a CUDA
+ * stream.  No torch types cross this boundary; the Python package
+ * `pridediff_gb300` binds it with ctypes, and a cgo / JNI / N-API binding
+ * would bind the same symbols.
+ *
+ * Differences from the reference boundary, all deliberate:
+ *  - geometry is a host POD (`dd_geom2d`, `dd_geom3d`) holding exactly the
+ *    entries of deeprecon's `options` tensor (projector.py:113, :286, :460),
+ *    instead of a device tensor read with 11-17 `.item()` syncs per call
+ *    (RadonTorch.cpp:19-29);
+ *  - work is enqueued on the caller's stream (the reference launches on the
+ *    legacy default stream and never checks for errors);
+ *  - the library never allocates: scratch comes from the caller through
+ *    `workspace` (size from the matching *_workspace_bytes query), so every
+ *    call is capturable in a CUDA graph;
+ *  - every entry returns a status code (DD_OK = 0) and never aborts.
+ *
+ * Layouts (all FP32, contiguous, row-major, as in the reference):
+ *   2-D image (B, H, W), sinogram (B, V, D)            RadonTorch.cpp:33, :68
+ *   3-D volume (B, Dep, H, W), sinogram (B, V, R, C)   RadonTorch.cpp:594, :631
+ *   angles (V) on the device; spiral source table (4, V) on the device with
+ *   rows [axial position, radius shift, angle shift, axial shift]
+ *   (RadonTorch.cpp:1040-1043).
+ * B is the product of the reference's batch and channel sizes.
+ */
+#ifndef PRIDEDIFF_DD_H
+#define PRIDEDIFF_DD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without requiring the CUDA headers */
+typedef struct CUstream_st *dd_stream_t;
+
+/* status codes */
+enum {
+    DD_OK = 0,
+    DD_ERR_INVALID_ARG = 1,   /* null pointer, non-positive or NaN geometry  */
+    DD_ERR_SIZE_OVERFLOW = 2, /* sizes overflow the 32-bit index space      */
+    DD_ERR_WORKSPACE = 3,     /* workspace missing or too small             */
+    DD_ERR_LAUNCH = 4,        /* a CUDA launch or runtime call failed       */
+    DD_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up         */
+    DD_ERR_UNSUPPORTED = 6    /* operator not defined for this geometry     */
+};
+
+/* scan geometry (projector scan_type) */
+enum { DD_SCAN_PARA = 0, DD_SCAN_FLAT = 1, DD_SCAN_ARC = 2 };
+enum { DD_SCAN_CONE_FLAT = 0, DD_SCAN_CONE_ARC = 1, DD_SCAN_SPIRAL = 2 };
+
+/* operators (RadonTorch.cpp:1375-1418) */
+enum {
+    DD_OP_PROJ = 0,     /* Proj*:                  image -> sinogram (A)          */
+    DD_OP_PROJ_T = 1,   /* ProjTrans*:             sinogram -> image (A^T, exact) */
+    DD_OP_BPROJ = 2,    /* BackProj*:              sinogram -> image (DD-BP)      */
+    DD_OP_BPROJ_T = 3,  /* BackProjTrans*:         image -> sinogram              */
+    DD_OP_BPROJ_W = 4,  /* BackProjWeighted*:      FBP-weighted DD-BP             */
+    DD_OP_BPROJ_TW = 5  /* BackProjTransWeighted*: its transpose                  */
+};
+
+/* 2-D geometry: the 11 entries of projector2d.options (projector.py:113).
+ * For fan-arc, det_size and bin_shift are angles (projector.py:110-112). */
+typedef struct dd_geom2d {
+    int width, height, num_det;
+    float pix_x, pix_y, det_size, iso_source, source_detector;
+    float pix_xshift, pix_yshift, bin_shift;
+} dd_geom2d;
+
+/* 3-D geometry: the 17 entries of projector3d.options (projector.py:286);
+ * projectorsp has no z shift (projector.py:460), pass pix_zshift = 0. */
+typedef struct dd_geom3d {
+    int width, height, depth, num_col, num_row;
+    float pix_x, pix_y, pix_z, col_size, row_size, iso_source, source_detector;
+    float pix_xshift, pix_yshift, pix_zshift, col_shift, row_shift;
+} dd_geom3d;
+
+/* ---- 2-D: generic entry --------------------------------------------------
+ * in/out/angles are device pointers; out is fully overwritten.
+ * Replaces the 16 2-D radontorch operators, e.g. ProjFanFlatDis2d
+ * (RadonTorch.cpp:17-49) for scan=DD_SCAN_FLAT, op=DD_OP_PROJ. */
+size_t dd2d_workspace_bytes(int scan, int op, const dd_geom2d *g, int batch, int num_view);
+int dd2d_apply(int scan, int op, const dd_geom2d *g, const float *in, float *out,
+               const float *angles, int batch, int num_view, void *workspace,
+               size_t workspace_bytes, dd_stream_t stream);
+
+/* ---- 2-D: geometry plan reuse ------------------------------------------
+ * The per-view / per-line geometry (detector boundary tables and the drifted
+ * pixel-boundary pieces) depends only on (scan, geometry, angles).  Building
+ * it once and passing it to dd2d_apply_planned saves the set-up kernels in
+ * iterative loops (and keeps them out of captured graphs). */
+size_t dd2d_plan_bytes(int scan, const dd_geom2d *g, int num_view);
+int dd2d_plan(int scan, const dd_geom2d *g, const float *angles, int num_view, void *plan,
+              size_t plan_bytes, dd_stream_t stream);
+size_t dd2d_apply_workspace_bytes(int scan, int op, const dd_geom2d *g, int batch, int num_view);
+int dd2d_apply_planned(int scan, int op, const dd_geom2d *g, const void *plan, const float *in,
+                       float *out, int batch, int num_view, void *workspace,
+                       size_t workspace_bytes, dd_stream_t stream);
+
+/* ---- 2-D: named entries, one per radontorch function --------------------
+ * Same arguments as dd2d_apply without scan/op.  Each replaces the pybind
+ * function of the same name (RadonTorch.cpp:1376-1393). */
+#define DD_NAMED2D(name)                                                            \
+    int dd_##name(const dd_geom2d *g, const float *in, float *out, const float *angles, \
+                  int batch, int num_view, void *workspace, size_t workspace_bytes,      \
+                  dd_stream_t stream)
+DD_NAMED2D(ProjFanFlatDis2d);               /* RadonTorch.cpp:17   */
+DD_NAMED2D(ProjTransFanFlatDis2d);          /* RadonTorch.cpp:52   */
+DD_NAMED2D(BackProjFanFlatDis2d);           /* RadonTorch.cpp:86   */
+DD_NAMED2D(BackProjTransFanFlatDis2d);      /* RadonTorch.cpp:120  */
+DD_NAMED2D(BackProjWeightedFanFlatDis2d);   /* RadonTorch.cpp:154  */
+DD_NAMED2D(BackProjTransWeightedFanFlatDis2d); /* RadonTorch.cpp:188 */
+DD_NAMED2D(ProjFanArcDis2d);                /* RadonTorch.cpp:225  */
+DD_NAMED2D(ProjTransFanArcDis2d);           /* RadonTorch.cpp:260  */
+DD_NAMED2D(BackProjFanArcDis2d);            /* RadonTorch.cpp:294  */
+DD_NAMED2D(BackProjTransFanArcDis2d);       /* RadonTorch.cpp:328  */
+DD_NAMED2D(BackProjWeightedFanArcDis2d);    /* RadonTorch.cpp:362  */
+DD_NAMED2D(BackProjTransWeightedFanArcDis2d); /* RadonTorch.cpp:396 */
+DD_NAMED2D(ProjParaDis2d);                  /* RadonTorch.cpp:433  */
+DD_NAMED2D(ProjTransParaDis2d);             /* RadonTorch.cpp:468  */
+DD_NAMED2D(BackProjParaDis2d);              /* RadonTorch.cpp:502  */
+DD_NAMED2D(BackProjTransParaDis2d);         /* RadonTorch.cpp:536  */
+#undef DD_NAMED2D
+
+/* ---- diagnostics ---------------------------------------------------------- */
+const char *dd_status_string(int status);
+/* Library version and build target, e.g. "pridediff_dd 0.1 sm_103a". */
+const char *dd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRIDEDIFF_DD_H */

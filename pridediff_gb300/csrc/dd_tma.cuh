@@ -1,0 +1,60 @@
+// Bulk-copy (TMA) and mbarrier helpers for sm_100-family GPUs, as inline PTX.
+//
+// Every wait is bounded: a wait that does not complete within
+// DD_WAIT_LIMIT polls reports failure instead of spinning forever, and the
+// kernel records DD_ERR_TIMEOUT in its status word and returns.
+#pragma once
+
+#include <stdint.h>
+
+#ifndef DD_WAIT_LIMIT
+#define DD_WAIT_LIMIT (1u << 26)
+#endif
+
+__device__ __forceinline__ uint32_t dd_smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void dd_mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(dd_smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void dd_fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void dd_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(dd_smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion signalled on `bar`.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void dd_bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dd_smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(dd_smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool dd_mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}" : "=r"(ok)
+        : "r"(dd_smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity.  Returns false on timeout.
+__device__ __forceinline__ bool dd_mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < DD_WAIT_LIMIT; ++it) {
+        if (dd_mbar_try_wait(bar, parity)) return true;
+        if (it > 64) __nanosleep(32);
+    }
+    return false;
+}
