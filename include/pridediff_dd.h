@@ -82,6 +82,12 @@ typedef struct dd_geom3d {
     float pix_xshift, pix_yshift, pix_zshift, col_shift, row_shift;
 } dd_geom3d;
 
+/* ---- 2-D: argument validation (no device work) ---------------------------
+ * The checks every 2-D entry performs before enqueuing anything: returns
+ * DD_ERR_INVALID_ARG / DD_ERR_SIZE_OVERFLOW / DD_ERR_UNSUPPORTED or DD_OK.
+ * The reference checks only device and contiguity (RadonTorch.cpp:12-14). */
+int dd2d_validate(int scan, int op, const dd_geom2d *g, int batch, int num_view);
+
 /* ---- 2-D: generic entry --------------------------------------------------
  * in/out/angles are device pointers; out is fully overwritten.
  * Replaces the 16 2-D radontorch operators, e.g. ProjFanFlatDis2d
@@ -129,7 +135,18 @@ DD_NAMED2D(BackProjParaDis2d);              /* RadonTorch.cpp:502  */
 DD_NAMED2D(BackProjTransParaDis2d);         /* RadonTorch.cpp:536  */
 #undef DD_NAMED2D
 
-/* ---- diagnostics ---------------------------------------------------------- */
+/* ---- diagnostics ----------------------------------------------------------
+ * No counterpart in the reference (it has no instrumentation).  Kernel kinds
+ * for dd_profile_read: */
+enum { DD_KERNEL_FORWARD = 0, DD_KERNEL_ADJOINT = 1, DD_KERNEL_TABLES = 2, DD_KERNEL_PLAN = 3 };
+/* Number of kernels this library has launched in the process. */
+unsigned long long dd_launch_count(void);
+/* Record CUDA events around every subsequent launch (and reset the records);
+ * must not be enabled while a stream is being captured. */
+int dd_profile_enable(int on);
+/* Sum of the recorded durations (ms) and launch count of one kernel kind;
+ * synchronises on the recorded events. */
+int dd_profile_read(int kind, double *total_ms, int *count);
 const char *dd_status_string(int status);
 /* Library version and build target, e.g. "pridediff_dd 0.1 sm_103a". */
 const char *dd_version(void);

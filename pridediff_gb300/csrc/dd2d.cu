@@ -640,6 +640,36 @@ static int launch_status() {
     return e == cudaSuccess ? DD_OK : DD_ERR_LAUNCH;
 }
 
+// ---------------------------------------------------------------------------
+// Launch accounting and optional per-kernel event timing (benchmarks only;
+// never enabled during graph capture)
+// ---------------------------------------------------------------------------
+static unsigned long long g_launches = 0;
+static int g_prof = 0;
+struct ProfRec {
+    cudaEvent_t a, b;
+    int kind;
+};
+static ProfRec g_prof_rec[8192];
+static int g_prof_used = 0;
+static int g_prof_created = 0;
+
+static ProfRec *prof_begin(int kind, cudaStream_t st) {
+    if (!g_prof || g_prof_used >= 8192) return nullptr;
+    ProfRec *r = &g_prof_rec[g_prof_used];
+    if (g_prof_used >= g_prof_created) {
+        if (cudaEventCreate(&r->a) != cudaSuccess || cudaEventCreate(&r->b) != cudaSuccess) return nullptr;
+        g_prof_created++;
+    }
+    g_prof_used++;
+    r->kind = kind;
+    cudaEventRecord(r->a, st);
+    return r;
+}
+static void prof_end(ProfRec *r, cudaStream_t st) {
+    if (r) cudaEventRecord(r->b, st);
+}
+
 int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, size_t bytes,
          cudaStream_t st) {
     const PlanLayout P = plan_layout(scan, g, V);
@@ -652,9 +682,12 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
     float *bc = (float *)(base + P.bcoef);
     DdLine *lines = (DdLine *)(base + P.lines);
     DdLine *dlines = scan == DD_SCAN_PARA ? (DdLine *)(base + P.dlines) : nullptr;
+    ProfRec *pr = prof_begin(DD_KERNEL_PLAN, st);
     k_views<<<V, 256, 0, st>>>(geom, *g, angles, V, views, (float *)(base + P.ang), dp, bc);
     dim3 gl((P.nl + 63) / 64, V);
     k_lines<<<gl, 64, 0, st>>>(geom, *g, angles, V, P.nl, views, dp, lines, dlines);
+    prof_end(pr, st);
+    g_launches += 2;
     return launch_status();
 }
 
@@ -674,8 +707,11 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     auto kern = k_fwd<GEOM, 0>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
+    ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
     kern<<<grid, kThreads, S.total, st>>>(*g, op, B, V, P.nl, views, dp, bc, lines, dlines, tx, ty,
                                           out, status);
+    prof_end(pr, st);
+    g_launches++;
     return launch_status();
 }
 
@@ -688,12 +724,15 @@ static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const float *dp = (const float *)(planb + P.dp);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
+    ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
     if (op == DD_OP_PROJ_T)
         k_adj<GEOM, 0><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
     else if (op == DD_OP_BPROJ)
         k_adj<GEOM, 1><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
     else
         k_adj<GEOM, 2><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
+    prof_end(pr, st);
+    g_launches++;
     return launch_status();
 }
 
@@ -712,8 +751,11 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
     if (op_is_forward(op)) {
         float2 *tx = (float2 *)(wb + A.tabx), *ty = (float2 *)(wb + A.taby);
         const int nw = B * H;
+        ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
         k_tab_rows<<<(nw * 32 + 255) / 256, 256, 0, st>>>(in, B, H, W, tx);
         k_tab_cols<<<(B * W + 127) / 128, 128, 0, st>>>(in, B, H, W, ty);
+        prof_end(pr, st);
+        g_launches += 2;
         if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
         if (geom == DD_GEOM_PARA) return launch_fwd<DD_GEOM_PARA>(op, g, P, planb, B, V, tx, ty, out, status, st);
         if (geom == DD_GEOM_FLAT) return launch_fwd<DD_GEOM_FLAT>(op, g, P, planb, B, V, tx, ty, out, status, st);
@@ -723,10 +765,13 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
     const int mode = (op == DD_OP_PROJ_T) ? 0 : 1;
     const float pcx = g->pix_y / g->det_size, pcy = g->pix_x / g->det_size;
     const int nw = B * V;
+    ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
+    g_launches++;
     k_dettab<<<(nw * 32 + 255) / 256, 256, 0, st>>>(geom, mode, in, B, V, g->num_det,
                                                      (const DdView2 *)(planb + P.views),
                                                      (const float *)(planb + P.dp),
                                                      (const float *)(planb + P.bcoef), pcx, pcy, dtab);
+    prof_end(pr, st);
     if (geom == DD_GEOM_PARA) return launch_adj<DD_GEOM_PARA>(op, g, P, planb, angles, B, V, dtab, out, st);
     if (geom == DD_GEOM_FLAT) return launch_adj<DD_GEOM_FLAT>(op, g, P, planb, angles, B, V, dtab, out, st);
     return launch_adj<DD_GEOM_ARC>(op, g, P, planb, angles, B, V, dtab, out, st);
@@ -738,6 +783,10 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
 // C ABI
 // ---------------------------------------------------------------------------
 using namespace dd2;
+
+extern "C" int dd2d_validate(int scan, int op, const dd_geom2d *g, int batch, int num_view) {
+    return validate(scan, op, g, batch, num_view);
+}
 
 extern "C" size_t dd2d_plan_bytes(int scan, const dd_geom2d *g, int num_view) {
     if (!g || num_view <= 0) return 0;
@@ -827,3 +876,28 @@ extern "C" const char *dd_status_string(int status) {
 }
 
 extern "C" const char *dd_version(void) { return "pridediff_dd 0.1 sm_103a"; }
+
+extern "C" unsigned long long dd_launch_count(void) { return g_launches; }
+
+extern "C" int dd_profile_enable(int on) {
+    g_prof = on ? 1 : 0;
+    g_prof_used = 0;
+    return DD_OK;
+}
+
+extern "C" int dd_profile_read(int kind, double *total_ms, int *count) {
+    if (!total_ms || !count) return DD_ERR_INVALID_ARG;
+    double t = 0.0;
+    int n = 0;
+    for (int i = 0; i < g_prof_used; i++) {
+        if (g_prof_rec[i].kind != kind) continue;
+        if (cudaEventSynchronize(g_prof_rec[i].b) != cudaSuccess) return DD_ERR_LAUNCH;
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, g_prof_rec[i].a, g_prof_rec[i].b) != cudaSuccess) return DD_ERR_LAUNCH;
+        t += ms;
+        n++;
+    }
+    *total_ms = t;
+    *count = n;
+    return DD_OK;
+}

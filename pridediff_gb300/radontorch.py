@@ -1,0 +1,198 @@
+"""Drop-in for deeprecon's ``radontorch`` extension module.
+
+Exposes the same 39 functions with the same tensor semantics as the pybind
+module in deeprecon/interface/RadonTorch.cpp:1375-1418:
+
+* ``Op(input, options, angles[, source_pos]) -> Tensor``;
+* outputs are freshly allocated on the input's device and fully written;
+* inputs must share a device and be contiguous (RadonTorch.cpp:12-14);
+  violations raise ``RuntimeError`` like ``AT_ASSERTM`` does;
+* batch and channel dimensions are folded together (RadonTorch.cpp:30-37).
+
+Deliberate differences (all in the caller's favour):
+
+* the compute runs in ``libpridediff_dd.so`` on the current CUDA stream;
+  CPU tensors raise ``RuntimeError`` (the build has no CPU fallback);
+* ``options`` is read on the host once per (tensor, version) and cached, so
+  repeated calls do not synchronise with the device (the reference calls
+  ``.item()`` 11-17 times per call, RadonTorch.cpp:19-29);
+* launch and argument errors are reported (the reference checks none).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _native as N
+
+# ---------------------------------------------------------------------------
+# options on the host
+# ---------------------------------------------------------------------------
+_opt_cache: dict = {}
+
+
+def host_options(options):
+    """Python floats of an options vector without re-reading device memory."""
+    if isinstance(options, (list, tuple)):
+        return [float(x) for x in options]
+    if not isinstance(options, torch.Tensor):
+        raise RuntimeError("options must be a tensor or a sequence of numbers")
+    key = (options.data_ptr(), options._version, options.numel(), str(options.device))
+    hit = _opt_cache.get(key)
+    if hit is not None:
+        return hit
+    vals = [float(x) for x in options.detach().to("cpu", torch.float64).reshape(-1).tolist()]
+    if len(_opt_cache) > 256:
+        _opt_cache.clear()
+    _opt_cache[key] = vals
+    return vals
+
+
+def _check_inputs(x: torch.Tensor, angles: torch.Tensor, extra=None):
+    # CHECK_DEVICE / CHECK_CONTIGUOUS (RadonTorch.cpp:12-14)
+    tensors = [x, angles] + ([extra] if extra is not None else [])
+    dev = x.device
+    if any(t.device != dev for t in tensors):
+        raise RuntimeError("Expected all tensors to be on the same device")
+    if any(not t.is_contiguous() for t in tensors):
+        raise RuntimeError("Expected all tensors to be contiguous")
+    if dev.type != "cuda":
+        raise RuntimeError("pridediff_gb300 runs on CUDA devices only; got a tensor on " + str(dev))
+    if x.dtype != torch.float32 or angles.dtype != torch.float32:
+        raise RuntimeError("Expected float32 tensors")
+
+
+def _stream_ptr(dev):
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+class _PlanCache:
+    """Geometry plans keyed by (scan, geometry, angles tensor identity/version).
+
+    A plan holds the per-view detector tables and the per-line drift pieces;
+    it depends only on the geometry and the angles, so iterative callers (the
+    data-consistency loop, autograd forward + backward) build it once.  The
+    entry keeps a weak reference to the angles tensor so a new tensor that
+    happens to reuse the same memory is never mistaken for the old one.
+    """
+
+    def __init__(self, size: int = 8):
+        self.size = size
+        self.entries = []   # (key, weakref(angles), version, plan tensor)
+
+    def get(self, key, angles, build):
+        import weakref
+        for i, (k, ref, ver, plan) in enumerate(self.entries):
+            if k == key and ref() is angles and ver == angles._version:
+                self.entries.insert(0, self.entries.pop(i))
+                return plan
+        plan = build()
+        self.entries.insert(0, (key, weakref.ref(angles), angles._version, plan))
+        del self.entries[self.size:]
+        return plan
+
+    def clear(self):
+        self.entries.clear()
+
+
+plans = _PlanCache()
+
+
+def plan2d(scan: str, g, angles: torch.Tensor):
+    """Device plan of a 2-D geometry (cached)."""
+    lib = N.load()
+    sc = N.SCAN2D[scan]
+    V = int(angles.shape[0])
+    key = ("2d", sc, tuple(getattr(g, f) for f, _ in g._fields_), V, angles.device.index)
+
+    def build():
+        nbytes = int(lib.dd2d_plan_bytes(sc, g, V))
+        plan = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=angles.device)
+        N.check(lib.dd2d_plan(sc, g, angles.data_ptr(), V, plan.data_ptr(), nbytes,
+                              _stream_ptr(angles.device)), f"{scan} plan")
+        return plan
+
+    return plans.get(key, angles, build)
+
+
+def _apply2d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor) -> torch.Tensor:
+    _check_inputs(x, angles)
+    lib = N.load()
+    o = host_options(options)
+    g = N.geom2d(o)
+    if x.dim() != 4:
+        raise RuntimeError("expected a 4-D (B, C, ., .) tensor")
+    B, C = x.shape[0], x.shape[1]
+    V = angles.shape[0]
+    image_in = op in ("proj", "bproj_t", "bproj_tw")
+    if image_in:
+        if (x.shape[2], x.shape[3]) != (g.height, g.width):
+            raise RuntimeError("image size inconsistent with options")
+        out = torch.empty((B, C, V, g.num_det), dtype=torch.float32, device=x.device)
+    else:
+        if (x.shape[2], x.shape[3]) != (V, g.num_det):
+            raise RuntimeError("sinogram size inconsistent with options and angles")
+        out = torch.empty((B, C, g.height, g.width), dtype=torch.float32, device=x.device)
+    if B * C == 0:
+        return out.zero_()
+    sc, opc = N.SCAN2D[scan], N.OPS[op]
+    with torch.cuda.device(x.device):
+        # the library validates the geometry before anything is enqueued
+        N.check(lib.dd2d_validate(sc, opc, g, B * C, V), f"{scan} {op}")
+        plan = plan2d(scan, g, angles)
+        nbytes = int(lib.dd2d_apply_workspace_bytes(sc, opc, g, B * C, V))
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+        st = lib.dd2d_apply_planned(sc, opc, g, plan.data_ptr(), x.data_ptr(), out.data_ptr(), B * C, V,
+                                    ws.data_ptr(), nbytes, _stream_ptr(x.device))
+    N.check(st, f"{scan} {op}")
+    return out
+
+
+def _not_yet(name):
+    def f(*args, **kwargs):
+        raise NotImplementedError(f"radontorch.{name} is not available in this build")
+    f.__name__ = name
+    return f
+
+
+# ---------------------------------------------------------------------------
+# 2-D operators (RadonTorch.cpp:1376-1393)
+# ---------------------------------------------------------------------------
+def _mk2(scan, op, name):
+    def f(input, options, angles):
+        return _apply2d(scan, op, input, options, angles)
+    f.__name__ = name
+    f.__doc__ = f"Replaces radontorch.{name} (deeprecon/interface/RadonTorch.cpp)."
+    return f
+
+
+_NAMES2D = {
+    "FanFlat": "flat", "FanArc": "arc",
+}
+for _n, _s in _NAMES2D.items():
+    for _pre, _op in (("Proj", "proj"), ("ProjTrans", "proj_t"), ("BackProj", "bproj"),
+                      ("BackProjTrans", "bproj_t"), ("BackProjWeighted", "bproj_w"),
+                      ("BackProjTransWeighted", "bproj_tw")):
+        _name = f"{_pre}{_n}Dis2d"
+        globals()[_name] = _mk2(_s, _op, _name)
+for _pre, _op in (("Proj", "proj"), ("ProjTrans", "proj_t"), ("BackProj", "bproj"),
+                  ("BackProjTrans", "bproj_t")):
+    _name = f"{_pre}ParaDis2d"
+    globals()[_name] = _mk2("para", _op, _name)
+
+# ---------------------------------------------------------------------------
+# 3-D operators (RadonTorch.cpp:1395-1414) -- provided by the 3-D library
+# ---------------------------------------------------------------------------
+NAMES3D = [f"{pre}{geo}Dis3d" for geo in ("ConeFlat", "ConeArc", "Spiral")
+           for pre in ("Proj", "ProjTrans", "BackProj", "BackProjTrans", "BackProjWeighted",
+                       "BackProjTransWeighted")]
+for _name in NAMES3D:
+    globals()[_name] = _not_yet(_name)
+
+# ---------------------------------------------------------------------------
+# System matrices (RadonTorch.cpp:1270-1372)
+# ---------------------------------------------------------------------------
+for _name in ("GetSysMatrixFanFlat2d", "GetSysMatrixFanArc2d", "GetSysMatrixPara2d"):
+    globals()[_name] = _not_yet(_name)
+
+NAMES2D = [n for n in globals() if n.endswith("Dis2d")]
+ALL_NAMES = NAMES2D + NAMES3D + ["GetSysMatrixFanFlat2d", "GetSysMatrixFanArc2d", "GetSysMatrixPara2d"]

@@ -1,0 +1,106 @@
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden", "dd2d_golden.npz")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
+
+
+def pytest_collection_modifyitems(config, items):
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        return
+    skip = pytest.mark.skip(reason="no CUDA GPU")
+    for it in items:
+        if "gpu" in it.keywords:
+            it.add_marker(skip)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (nb if nb > 0 else 1.0))
+
+
+@pytest.fixture(scope="session")
+def golden():
+    return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    import oracle
+    oracle.build()
+    return oracle
+
+
+class _G2(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("num_det", ctypes.c_int)] + \
+        [(n, ctypes.c_float) for n in ("pix_x", "pix_y", "det_size", "iso_source", "source_detector",
+                                        "pix_xshift", "pix_yshift", "bin_shift")]
+
+
+class HostModel:
+    """ctypes wrapper of tests/native/dd_model2d.cpp (host model of the kernels)."""
+    OPS = {"proj": 0, "proj_t": 1, "bproj": 2, "bproj_t": 3, "bproj_w": 4}
+    SCAN = {"para": 0, "flat": 1, "arc": 2}
+
+    def __init__(self, path):
+        self.lib = ctypes.CDLL(path)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self.lib.model_apply2d.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_G2), fp, fp, fp,
+                                           ctypes.c_int, ctypes.c_int]
+        self.lib.model_check_pieces.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_float)]
+
+    def apply2d(self, geom, op, x, angles, opt):
+        fp = ctypes.POINTER(ctypes.c_float)
+        g = _G2(int(opt[0]), int(opt[1]), int(opt[2]), *[float(v) for v in opt[3:]])
+        V = len(angles)
+        B = x.shape[0]
+        shape = (B, V, int(opt[2])) if op in ("proj", "bproj_t") else (B, int(opt[1]), int(opt[0]))
+        out = np.zeros(shape, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        a = np.ascontiguousarray(angles, np.float32)
+        rc = self.lib.model_apply2d(self.SCAN[geom], self.OPS[op], ctypes.byref(g), x.ctypes.data_as(fp),
+                                    out.ctypes.data_as(fp), a.ctypes.data_as(fp), B, V)
+        assert rc == 0
+        return out
+
+    def check_pieces(self, v0, pint, i0, nend):
+        npc, fl, dev = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        bad = self.lib.model_check_pieces(ctypes.c_float(v0), ctypes.c_float(pint), i0, nend,
+                                          ctypes.byref(npc), ctypes.byref(fl), ctypes.byref(dev))
+        return bad, npc.value, fl.value, dev.value
+
+
+@pytest.fixture(scope="session")
+def host_model():
+    src = os.path.join(ROOT, "tests", "native", "dd_model2d.cpp")
+    outdir = os.path.join(ROOT, "tests", "native", "_build")
+    os.makedirs(outdir, exist_ok=True)
+    so = os.path.join(outdir, "libddmodel2d.so")
+    hdrs = [os.path.join(ROOT, "pridediff_gb300", "csrc", f) for f in ("dd_geom.cuh", "dd_geom2d.cuh")]
+    if not os.path.exists(so) or any(os.path.getmtime(p) > os.path.getmtime(so) for p in [src] + hdrs):
+        r = subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src,
+                            "-o", so], capture_output=True, text=True)
+        if r.returncode != 0:
+            pytest.skip("host model does not compile here: " + r.stderr[-400:])
+    return HostModel(so)

@@ -1,0 +1,84 @@
+"""Generate the golden vectors under tests/golden/ from deeprecon's own CPU code.
+
+Run in a checkout where the reference sources exist (they are compiled into
+oracle/_ref/libddref.so by `make -C oracle`):
+
+    python tests/golden/make_golden.py
+
+Every case stores its seeded inputs and the reference outputs (computed by
+the unmodified deeprecon CPU projectors, single-threaded), so the tests can
+check the oracle and the CUDA path on machines where the reference cannot be
+built.  Cases are small (tens of KB each).
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle  # noqa: E402
+
+OPS2D = {"para": ["proj", "proj_t", "bproj", "bproj_t"],
+         "flat": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"],
+         "arc": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"]}
+
+# (name, geometry, options, angles): odd sizes, shifts and non-square pixels
+CASES = [
+    ("para_small", "para", [64, 48, 95, 1.0, 1.1, 1.0, 500.0, 1000.0, 0.3, -0.2, 0.25],
+     np.arange(90) * np.pi / 90),
+    ("flat_small", "flat", [64, 48, 80, 0.9, 0.8, 1.3, 595.0, 1085.6, 0.5, -0.4, 0.6],
+     np.arange(120) * 2 * np.pi / 120),
+    ("arc_small", "arc", [64, 48, 80, 0.9, 0.8, 1.3 / 1085.6, 595.0, 1085.6, 0.5, -0.4, 0.6 / 1085.6],
+     np.arange(120) * 2 * np.pi / 120),
+    ("flat_odd", "flat", [37, 53, 61, 1.7, 1.3, 2.1, 400.0, 800.0, -1.2, 0.7, -0.9],
+     np.linspace(0.1, 6.0, 47)),
+]
+
+
+def ellipse_phantom(h, w, n, rng, scale=1.0):
+    """Additive ellipses at pixel centres (the convention of deeprecon's phantom.py)."""
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    cy, cx = (h - 1) / 2.0, (w - 1) / 2.0
+    img = np.zeros((h, w))
+    for _ in range(n):
+        x0 = rng.uniform(-0.8, 0.8) * w / 2 + cx
+        y0 = rng.uniform(-0.8, 0.8) * h / 2 + cy
+        a, b = rng.uniform(2, max(3, w / 4)), rng.uniform(2, max(3, h / 4))
+        t = rng.uniform(0, np.pi)
+        dx, dy = xx - x0, yy - y0
+        u = dx * np.cos(t) + dy * np.sin(t)
+        v = -dx * np.sin(t) + dy * np.cos(t)
+        img[(u / a) ** 2 + (v / b) ** 2 <= 1] += rng.uniform(0, 1) * scale
+    return img.astype(np.float32)
+
+
+def main():
+    if not oracle.have_ref():
+        oracle.build()
+    if not oracle.have_ref():
+        raise SystemExit("reference sources not present: cannot regenerate golden vectors")
+    out = {}
+    for seed, (name, geom, opt, ang) in enumerate(CASES):
+        rng = np.random.default_rng(1000 + seed)
+        ang = ang.astype(np.float32)
+        W, H, D = opt[0], opt[1], opt[2]
+        img = np.stack([ellipse_phantom(H, W, 6, rng), rng.random((H, W)).astype(np.float32)])
+        sino = rng.standard_normal((2, len(ang), D)).astype(np.float32)
+        out[f"{name}/options"] = np.asarray(opt, np.float32)
+        out[f"{name}/angles"] = ang
+        out[f"{name}/image"] = img
+        out[f"{name}/sino"] = sino
+        for op in OPS2D[geom]:
+            x = img if op in oracle.IMAGE_INPUT else sino
+            out[f"{name}/{op}/ref"] = oracle.ref2d(geom, op, x, ang, opt)
+    path = os.path.join(HERE, "dd2d_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path) // 1024, "KB")
+
+
+if __name__ == "__main__":
+    main()

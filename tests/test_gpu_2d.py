@@ -1,0 +1,188 @@
+"""GPU parity of the 2-D operators (CUDA path through the C ABI).
+
+Bars: rel-L2 <= 1e-5 against deeprecon's CPU path (golden vectors and the
+FP32 oracle, which is bit-exact with it); dot-product adjointness <= 1e-6
+with FP64 accumulation.  Each test also records the error against the FP64
+oracle in its output.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+OPS = {"para": ["proj", "proj_t", "bproj", "bproj_t"],
+       "flat": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"],
+       "arc": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"]}
+NAMES = {"proj": "Proj{}Dis2d", "proj_t": "ProjTrans{}Dis2d", "bproj": "BackProj{}Dis2d",
+         "bproj_t": "BackProjTrans{}Dis2d", "bproj_w": "BackProjWeighted{}Dis2d",
+         "bproj_tw": "BackProjTransWeighted{}Dis2d"}
+GEO = {"para": "Para", "flat": "FanFlat", "arc": "FanArc"}
+IMAGE_IN = ("proj", "bproj_t", "bproj_tw")
+
+
+def run(geom, op, x, angles, opt):
+    from pridediff_gb300 import radontorch
+    fn = getattr(radontorch, NAMES[op].format(GEO[geom]))
+    xt = torch.from_numpy(np.ascontiguousarray(x)[:, None]).cuda()
+    at = torch.from_numpy(np.ascontiguousarray(angles, np.float32)).cuda()
+    out = fn(xt, torch.tensor(np.asarray(opt, np.float32)), at)
+    torch.cuda.synchronize()
+    return out[:, 0].cpu().numpy()
+
+
+def _cases():
+    for c in ["para_small", "flat_small", "arc_small", "flat_odd"]:
+        geom = c.split("_")[0]
+        for op in OPS[geom]:
+            yield c, geom, op
+
+
+@pytest.mark.parametrize("case,geom,op", list(_cases()))
+def test_gpu_matches_reference_golden(golden, oracle_mod, case, geom, op):
+    opt = golden[f"{case}/options"]
+    ang = golden[f"{case}/angles"]
+    x = golden[f"{case}/image"] if op in IMAGE_IN else golden[f"{case}/sino"]
+    out = run(geom, op, x, ang, opt)
+    ref = golden[f"{case}/{op}/ref"]
+    e_ref = rel_l2(out, ref)
+    e64 = rel_l2(out, oracle_mod.run2d(geom, op, x, ang, opt, "d", 0))
+    print(f"{case} {op}: rel-L2 vs reference {e_ref:.2e}, vs FP64 {e64:.2e}")
+    assert e_ref <= 1e-5
+
+
+def _phantom(h, w, n, rng, scale=1.0):
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    img = np.zeros((h, w))
+    for _ in range(n):
+        x0 = rng.uniform(-0.8, 0.8) * w / 2 + (w - 1) / 2
+        y0 = rng.uniform(-0.8, 0.8) * h / 2 + (h - 1) / 2
+        a, b = rng.uniform(5, 60), rng.uniform(5, 60)
+        t = rng.uniform(0, np.pi)
+        u = (xx - x0) * np.cos(t) + (yy - y0) * np.sin(t)
+        v = -(xx - x0) * np.sin(t) + (yy - y0) * np.cos(t)
+        img[(u / a) ** 2 + (v / b) ** 2 <= 1] += rng.uniform(0, 1) * scale
+    return img.astype(np.float32)
+
+
+C1 = ([256, 256, 367, 1.0, 1.0, 1.0, 500.0, 1000.0, 0.0, 0.0, 0.0],
+      (np.arange(180) * np.pi / 180).astype(np.float32))
+C2 = ([512, 512, 736, 0.66, 0.66, 1.2858, 595.0, 1085.6, 0.0, 0.0, 0.0],
+      (np.arange(720) * 2 * np.pi / 720).astype(np.float32))
+
+
+@pytest.mark.parametrize("op", ["proj", "proj_t"])
+def test_config1_parallel_full(oracle_mod, op):
+    opt, ang = C1
+    rng = np.random.default_rng(11)
+    x = _phantom(256, 256, 10, rng)[None] if op == "proj" else rng.standard_normal((1, 180, 367)).astype(np.float32)
+    out = run("para", op, x, ang, opt)
+    ref = oracle_mod.run2d("para", op, x, ang, opt, "f", 0)
+    e = rel_l2(out, ref)
+    e64 = rel_l2(out, oracle_mod.run2d("para", op, x, ang, opt, "d", 0))
+    print(f"c1 {op}: rel-L2 vs reference {e:.2e}, vs FP64 {e64:.2e}")
+    assert e <= 1e-5
+
+
+@pytest.mark.parametrize("op", ["proj", "proj_t", "bproj", "bproj_t"])
+def test_config2_fanflat_full_size(oracle_mod, op):
+    opt, ang = C2
+    rng = np.random.default_rng(12)
+    if op in IMAGE_IN:
+        x = np.stack([np.clip(_phantom(512, 512, 10, rng, 0.04), 0, 0.04) for _ in range(2)])
+    else:
+        x = rng.standard_normal((2, 720, 736)).astype(np.float32)
+    out = run("flat", op, x, ang, opt)
+    ref = oracle_mod.run2d("flat", op, x, ang, opt, "f", 0)
+    e = rel_l2(out, ref)
+    print(f"c2 {op}: rel-L2 vs reference {e:.2e}")
+    assert e <= 1e-5
+
+
+@pytest.mark.parametrize("geom", ["para", "flat", "arc"])
+def test_dot_product_adjointness(geom):
+    from pridediff_gb300 import radontorch
+    opt = {"para": C1[0], "flat": C2[0], "arc": [512, 512, 768, 0.66, 0.66, 1.2858 / 1085.6, 595.0,
+                                                  1085.6, 0.0, 0.0, 0.0]}[geom]
+    V = 360
+    ang = torch.arange(V, dtype=torch.float32, device="cuda") * (2 * np.pi / V)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.rand((2, 1, opt[1], opt[0]), device="cuda", generator=g)
+    y = torch.randn((2, 1, V, opt[2]), device="cuda", generator=g)
+    A = getattr(radontorch, f"Proj{GEO[geom]}Dis2d")
+    AT = getattr(radontorch, f"ProjTrans{GEO[geom]}Dis2d")
+    o = torch.tensor(opt, dtype=torch.float32)
+    lhs = (A(x, o, ang).double() * y.double()).sum().item()
+    rhs = (x.double() * AT(y, o, ang).double()).sum().item()
+    err = abs(lhs - rhs) / abs(lhs)
+    print(f"{geom}: dot-test {err:.2e}")
+    assert err <= 1e-6
+
+
+def test_autograd_gradient_matches_adjoint_and_fd():
+    import pridediff_gb300 as P
+    opt, ang_np = C2
+    proj = P.projector2d(512, 736, 0.66, 1.2858, 595.0, 1085.6).cuda()
+    ang = torch.from_numpy(ang_np).cuda()
+    rng = np.random.default_rng(21)
+    xt = np.clip(_phantom(512, 512, 10, rng, 0.04), 0, 0.04)
+    x = torch.from_numpy(xt[None, None]).cuda()
+    with torch.no_grad():
+        p = proj.projection(x, ang)
+        counts = torch.poisson(1e5 * torch.exp(-p.double()))
+        y = (-torch.log(torch.clamp(counts, min=1.0) / 1e5)).float()
+    x0 = (x * 0.9).requires_grad_(True)
+    loss = ((proj.projection(x0, ang) - y) ** 2).sum()
+    loss.backward()
+    with torch.no_grad():
+        gref = 2 * proj.projection_t(proj.projection(x0, ang) - y, ang)
+    assert rel_l2(x0.grad.cpu().numpy(), gref.cpu().numpy()) == 0.0
+    # central finite differences at 64 pixels (quadratic loss: no truncation error)
+    idx = rng.choice(512 * 512, 64, replace=False)
+    h = 1e-2 * float(x0.max())
+    base = x0.detach().clone()
+    fd = []
+    for k in idx:
+        e = torch.zeros_like(base).view(-1)
+        e[k] = h
+        e = e.view_as(base)
+        with torch.no_grad():
+            lp = ((proj.projection(base + e, ang) - y).double() ** 2).sum().item()
+            lm = ((proj.projection(base - e, ang) - y).double() ** 2).sum().item()
+        fd.append((lp - lm) / (2 * h))
+    ag = x0.grad.view(-1)[torch.from_numpy(idx).cuda()].double().cpu().numpy()
+    err = rel_l2(ag, np.array(fd))
+    print(f"FD vs autograd (64 pixels): {err:.2e}")
+    assert err <= 1e-3
+
+
+def test_deterministic_and_stream_ordered():
+    from pridediff_gb300 import radontorch
+    opt, ang_np = C2
+    ang = torch.from_numpy(ang_np).cuda()
+    o = torch.tensor(opt)
+    y = torch.randn((3, 1, 720, 736), device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        a = radontorch.ProjTransFanFlatDis2d(y, o, ang)
+        b = radontorch.ProjTransFanFlatDis2d(y, o, ang)
+    s.synchronize()
+    assert torch.equal(a, b)
+
+
+def test_errors_are_raised():
+    from pridediff_gb300 import radontorch
+    o = torch.tensor([64, 64, 90, 1, 1, 1, 500, 1000, 0, 0, 0], dtype=torch.float32)
+    ang = torch.zeros(10, device="cuda")
+    with pytest.raises(RuntimeError):
+        radontorch.ProjFanFlatDis2d(torch.zeros(1, 1, 64, 64), o, ang)          # CPU input
+    with pytest.raises(RuntimeError):
+        radontorch.ProjFanFlatDis2d(torch.zeros(1, 1, 64, 128, device="cuda")[..., ::2], o, ang)
+    with pytest.raises(RuntimeError):
+        radontorch.ProjFanFlatDis2d(torch.zeros(1, 1, 32, 64, device="cuda"), o, ang)
+    bad = o.clone()
+    bad[3] = float("nan")
+    with pytest.raises(RuntimeError):
+        radontorch.ProjFanFlatDis2d(torch.zeros(1, 1, 64, 64, device="cuda"), bad, ang)
