@@ -307,6 +307,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     float *dps = reinterpret_cast<float *>(smem + L.dp);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     __shared__ int abort_flag;
+    __shared__ float wsum[kWarps];
 
     const float2 *tsrc = xb ? tabx : taby;
     const size_t line_stride = (size_t)rs;                 // float2 per line
@@ -355,6 +356,67 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
         if (abort_flag) break;
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
+        if (WEIGHTED && np > 0) {
+            // BackProjTransWeighted: multiply every pixel by its FBP weight at
+            // this view (FanFlatDisCPU2d.cpp:693, FanArcDisCPU2d.cpp:703) and
+            // rebuild the line's prefix table in place (block scan).
+            float2 *tw = tab + (size_t)buf * kBI * rsmax;
+            const float lpos = xb
+                ? (float)(((double)g.height / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift)
+                : (float)(((double)line - g.width / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
+            for (int b = 0; b < nb; b++) {
+                float2 *t = tw + (size_t)b * rsmax;
+                constexpr int kPer = 16;   // npix <= 4096
+                const int per = (npix + kThreads - 1) / kThreads;
+                float yv[kPer];
+                float run = 0.0f;
+#pragma unroll
+                for (int q = 0; q < kPer; q++) {
+                    const int i = tid * per + q;
+                    float y = 0.0f;
+                    if (q < per && i < npix) {
+                        float pcx, pcy;
+                        if (xb) {
+                            pcx = (float)(((double)i + 0.5) * (double)g.pix_x + (double)vw.axis0);
+                            pcy = lpos;
+                        } else {
+                            pcx = lpos;
+                            pcy = (float)(((double)i + 0.5) * (double)g.pix_y + (double)vw.axis0);
+                        }
+                        const float w = (GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
+                                                              : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                        y = t[i].y * w;
+                    }
+                    yv[q] = y;
+                    run += y;
+                }
+                // exclusive scan of the per-thread sums across the block
+                float inc = run;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float z = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += z;
+                }
+                if (lane == 31) wsum[warp] = inc;
+                __syncthreads();
+                float wbase = 0.0f;
+                for (int w = 0; w < warp; w++) wbase += wsum[w];
+                float pre = wbase + inc - run;
+#pragma unroll
+                for (int q = 0; q < kPer; q++) {
+                    const int i = tid * per + q;
+                    if (q < per && i < npix) {
+                        t[i] = make_float2(pre, yv[q]);
+                        pre += yv[q];
+                    }
+                }
+                if (tid == kThreads - 1) {
+                    float tot = 0.0f;
+                    for (int w = 0; w < kWarps; w++) tot += wsum[w];
+                    t[npix] = make_float2(tot, 0.0f);
+                }
+                __syncthreads();
+            }
+        }
         if (np > 0) {
             const float2 *tb = tab + (size_t)buf * kBI * rsmax;
             // per-piece constants, one warp per image
@@ -456,14 +518,63 @@ __device__ __forceinline__ void det_index_fan(int geom, const dd_geom2d &g, cons
     *kk = min(max(k, 0), D - 1);
 }
 
+// Shared-memory layout of the adjoint kernel (bytes).
+struct AdjSmem {
+    int rec, drec, kd, bar, total;
+};
+
+__host__ __device__ inline AdjSmem adj_smem(int geom) {
+    AdjSmem s;
+    int o = 0;
+    s.rec = o; o += 2 * kTile * (int)sizeof(DdLine);
+    s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * kTile * (int)sizeof(DdLine);
+    s.kd = o; if (geom == DD_GEOM_PARA) o += kWarps * kBI * 32 * (int)sizeof(float);
+    s.bar = o; o += 2 * (int)sizeof(uint64_t);
+    // the final merge of the two pixel ownerships reuses the record buffers
+    const int merge = kBI * kTile * (kTile + 1) * (int)sizeof(float);
+    if (o < merge + 16) o = merge + 16;
+    s.total = (o + 127) & ~127;
+    return s;
+}
+
+// Detector-table position of axis value uu (fan beams): bin k with
+// d_k <= uu < d_{k+1} (corrected against the exact table), clamped to the
+// walked bins.  Returns k and d_k.
+__device__ __forceinline__ int fan_bin(int geom, const dd_geom2d &g, const DdView2 &vw, float view,
+                                       const float *__restrict__ dpv, float uu, int idet0, float *dk_out) {
+    const int D = g.num_det;
+    int k;
+    det_index_fan(geom, g, vw, view, uu, &k);
+    float dk = __ldg(dpv + k);
+    if (k > 0 && uu < dk) {
+        k--;
+        dk = __ldg(dpv + k);
+    } else if (k < D - 1 && uu >= __ldg(dpv + k + 1)) {
+        k++;
+        dk = __ldg(dpv + k);
+    }
+    if (k < idet0) {
+        k = idet0;
+        dk = __ldg(dpv + k);
+    }
+    *dk_out = dk;
+    return k;
+}
+
 template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
 __global__ void __launch_bounds__(kThreads)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const DdView2 *__restrict__ views, const float *__restrict__ dp,
       const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines,
-      const float2 *__restrict__ dtab, float *__restrict__ out) {
-    __shared__ float tile[kBI][kTile][kTile + 1];
-    __shared__ float kd[(GEOM == DD_GEOM_PARA) ? kWarps : 1][kBI][32];
+      const float2 *__restrict__ dtab, float *__restrict__ out, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const AdjSmem SL = adj_smem(GEOM);
+    DdLine *recs = reinterpret_cast<DdLine *>(smem + SL.rec);
+    DdLine *drecs = reinterpret_cast<DdLine *>(smem + SL.drec);
+    float *kdp = reinterpret_cast<float *>(smem + SL.kd);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SL.bar);
+    __shared__ int abort_flag;
+
     const int c0 = blockIdx.x * kTile, r0 = blockIdx.y * kTile;
     const int b0 = blockIdx.z * kBI;
     const int nb = min(kBI, B - b0);
@@ -471,97 +582,72 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     const int W = g.width, H = g.height, D = g.num_det;
     const int rsd = rs_entries(D);
 
+    if (tid == 0) {
+        abort_flag = 0;
+        dd_mbar_init(&bar[0], 1);
+        dd_mbar_init(&bar[1], 1);
+        dd_fence_mbar_init();
+    }
+    __syncthreads();
+
+    // records of the tile's lines of view v: rows r0.. (x-branch) or columns c0..
+    auto issue = [&](int v, int buf) {
+        const int xbv = views[v].xb;
+        const int line0 = xbv ? r0 : c0;
+        const int nline = xbv ? H : W;
+        const int n = min(kTile, nline - line0);
+        const uint32_t bytes = (uint32_t)(n * sizeof(DdLine));
+        dd_mbar_expect_tx(&bar[buf], bytes * (GEOM == DD_GEOM_PARA ? 2u : 1u));
+        dd_bulk_g2s(recs + buf * kTile, lines + (size_t)v * nl + line0, bytes, &bar[buf]);
+        if (GEOM == DD_GEOM_PARA)
+            dd_bulk_g2s(drecs + buf * kTile, dlines + (size_t)v * nl + line0, bytes, &bar[buf]);
+    };
+
     float ax[kLinesPerWarp][kBI], ay[kLinesPerWarp][kBI];
 #pragma unroll
     for (int q = 0; q < kLinesPerWarp; q++)
 #pragma unroll
         for (int b = 0; b < kBI; b++) ax[q][b] = ay[q][b] = 0.0f;
 
+    if (tid == 0) issue(0, 0);
     for (int v = 0; v < V; v++) {
+        const int buf = v & 1;
+        if (tid == 0 && v + 1 < V) issue(v + 1, buf ^ 1);
+        if (!dd_mbar_wait(&bar[buf], (v >> 1) & 1)) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
         const DdView2 vw = views[v];
         const float view = angles[v];
         const float *dpv = dp + (size_t)v * (D + 1);
         const float dend = (GEOM == DD_GEOM_PARA) ? 0.0f : __ldg(dpv + D);
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) {
-            // line and pixel index along it for this lane
+            const int rel = warp + kWarps * q;
             int line, pi;
             if (vw.xb) {
-                line = r0 + warp + kWarps * q;
+                line = r0 + rel;
                 pi = c0 + lane;
                 if (line >= H) continue;
             } else {
-                line = c0 + warp + kWarps * q;
+                line = c0 + rel;
                 pi = H - r0 - kTile + lane;
                 if (line >= W) continue;
             }
-            const DdLine &L = lines[(size_t)v * nl + line];
+            const DdLine &L = recs[buf * kTile + rel];
             const int np = L.h.npiece;
             if (np == 0) continue;   // warp-uniform
             const int i0 = L.h.i0, nend = L.h.nend;
             const float bound0 = L.h.bound0;
             const int idet0 = L.h.idet0;
             const bool valid = (pi >= i0) && (pi < nend) && (pi >= 0);
-            // boundary values: upper of pixel pi, and lower for lane 0 / first pixel
-            float up = bound0;
-            if (valid) {
-                const float est = L.p[0].Q + (float)(pi - L.p[0].gb) * L.p[0].dl;
-                up = dd_boundary(&L, pi, est);
-            }
-            const DdLine *Ld = nullptr;
-            if (GEOM == DD_GEOM_PARA) {
-                Ld = &dlines[(size_t)v * nl + line];
-                // per-piece constants of the detector integral, lane = piece
-                const bool has = Ld->h.npiece > 0;
-                for (int b = 0; b < nb; b++) {
-                    const float Kb = has ? piece_K(*Ld, dtab + ((size_t)(b0 + b) * V + v) * rsd, lane) : 0.0f;
-                    kd[(GEOM == DD_GEOM_PARA) ? warp : 0][b][lane] = Kb;
-                }
-                __syncwarp();
-            }
-            auto Hval = [&](float u, int b) -> float {
-                const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;
-                if (GEOM == DD_GEOM_PARA) {
-                    if (Ld->h.npiece == 0) return 0.0f;
-                    const float uu = fminf(fmaxf(u, bound0), Ld->h.endv);
-                    int p, j;
-                    float r;
-                    dd_locate(Ld, uu, &p, &j, &r);
-                    const float Kp = kd[(GEOM == DD_GEOM_PARA) ? warp : 0][b][p];
-                    const float2 e = __ldg(t + j);
-                    return fmaf(r, e.y, fmaf(Ld->p[p].dl, e.x, Kp));
-                } else {
-                    const float uu = fminf(fmaxf(u, bound0), dend);
-                    int k;
-                    det_index_fan(GEOM, g, vw, view, uu, &k);
-                    // one-step correction against the exact boundary table
-                    float dk = __ldg(dpv + k);
-                    if (k > 0 && uu < dk) {
-                        k--;
-                        dk = __ldg(dpv + k);
-                    } else if (k < D - 1 && uu >= __ldg(dpv + k + 1)) {
-                        k++;
-                        dk = __ldg(dpv + k);
-                    }
-                    if (k < idet0) {
-                        k = idet0;
-                        dk = __ldg(dpv + k);
-                    }
-                    const float2 e = __ldg(t + k);
-                    return fmaf(uu - dk, e.y, e.x);
-                }
-            };
-            // lower boundary: previous lane's upper; lane 0 and pixel i0 explicit
-            float lowx = bound0;
-            const bool need_low = valid && (lane == 0) && (pi > i0);
-            if (need_low) {
-                const float est = L.p[0].Q + (float)(pi - 1 - L.p[0].gb) * L.p[0].dl;
-                lowx = dd_boundary(&L, pi - 1, est);
-            }
+            const bool need_low = valid && (lane == 0 || pi == i0);
+            // image-independent geometry: boundary values and their detector positions
+            float up = bound0, low = bound0;
+            if (valid) up = dd_boundary(&L, pi, L.p[0].Q + (float)(pi - L.p[0].gb) * L.p[0].dl);
+            if (need_low && pi > i0) low = dd_boundary(&L, pi - 1, L.p[0].Q + (float)(pi - 1 - L.p[0].gb) * L.p[0].dl);
             const float alpha = (OPK == 0) ? 1.0f : L.h.alpha;
-            float wgt = 1.0f;
+            float wgt = alpha;
             if (OPK == 2 && valid) {
-                // pixel centre (FanFlatDisCPU2d.cpp:490 / :565)
                 float pcx, pcy;
                 if (vw.xb) {
                     pcx = (float)(((double)pi + 0.5) * (double)g.pix_x + (double)vw.axis0);
@@ -570,25 +656,95 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
                     pcx = (float)(((double)line - W / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
                     pcy = (float)(((double)pi + 0.5) * (double)g.pix_y + (double)vw.axis0);
                 }
-                wgt = (GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
-                                            : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                wgt = alpha * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
+                                                     : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
             }
+            if (GEOM == DD_GEOM_PARA) {
+                const DdLine &Ld = drecs[buf * kTile + rel];
+                const int npd = Ld.h.npiece;
+                float *kd = kdp + warp * kBI * 32;
+                for (int b = 0; b < nb; b++) {
+                    const float Kb = npd > 0 ? piece_K(Ld, dtab + ((size_t)(b0 + b) * V + v) * rsd, lane) : 0.0f;
+                    kd[b * 32 + lane] = Kb;
+                }
+                __syncwarp();
+                int pU = 0, jU = 0, pL = 0, jL = 0;
+                float rU = 0.0f, rL = 0.0f, dlU = 0.0f, dlL = 0.0f;
+                if (npd > 0) {
+                    const float uu = fminf(fmaxf(up, bound0), Ld.h.endv);
+                    dd_locate(&Ld, uu, &pU, &jU, &rU);
+                    dlU = Ld.p[pU].dl;
+                    const float ul = fminf(fmaxf(low, bound0), Ld.h.endv);
+                    dd_locate(&Ld, ul, &pL, &jL, &rL);
+                    dlL = Ld.p[pL].dl;
+                }
 #pragma unroll
-            for (int b = 0; b < kBI; b++) {
-                if (b >= nb) break;
-                const float hu = Hval(up, b);
-                float hl = __shfl_up_sync(0xffffffffu, hu, 1);
-                if (lane == 0 || pi == i0) hl = Hval((pi == i0) ? bound0 : lowx, b);
-                if (valid) {
-                    const float val = alpha * (hu - hl) * wgt;
-                    if (vw.xb) ax[q][b] += val;
-                    else ay[q][b] += val;
+                for (int b = 0; b < kBI; b++) {
+                    if (b >= nb) break;
+                    const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;
+                    float hu = 0.0f, hl2 = 0.0f;
+                    if (npd > 0) {
+                        const float2 e = __ldg(t + jU);
+                        hu = fmaf(rU, e.y, fmaf(dlU, e.x, kd[b * 32 + pU]));
+                        if (need_low) {
+                            const float2 e2 = __ldg(t + jL);
+                            hl2 = fmaf(rL, e2.y, fmaf(dlL, e2.x, kd[b * 32 + pL]));
+                        }
+                    }
+                    float hl = __shfl_up_sync(0xffffffffu, hu, 1);
+                    if (need_low) hl = hl2;
+                    if (valid) {
+                        const float val = wgt * (hu - hl);
+                        if (vw.xb) ax[q][b] += val;
+                        else ay[q][b] += val;
+                    }
+                }
+                __syncwarp();
+            } else {
+                const float uu = fminf(fmaxf(up, bound0), dend);
+                float dkU;
+                const int kU = fan_bin(GEOM, g, vw, view, dpv, uu, idet0, &dkU);
+                const float offU = uu - dkU;
+                int kL = kU;
+                float offL = 0.0f;
+                if (need_low) {
+                    const float ul = fminf(fmaxf(low, bound0), dend);
+                    float dkL;
+                    kL = fan_bin(GEOM, g, vw, view, dpv, ul, idet0, &dkL);
+                    offL = ul - dkL;
+                }
+#pragma unroll
+                for (int b = 0; b < kBI; b++) {
+                    if (b >= nb) break;
+                    const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;
+                    const float2 e = __ldg(t + kU);
+                    const float hu = fmaf(offU, e.y, e.x);
+                    float hl = __shfl_up_sync(0xffffffffu, hu, 1);
+                    if (need_low) {
+                        const float2 e2 = __ldg(t + kL);
+                        hl = fmaf(offL, e2.y, e2.x);
+                    }
+                    if (valid) {
+                        const float val = wgt * (hu - hl);
+                        if (vw.xb) ax[q][b] += val;
+                        else ay[q][b] += val;
+                    }
                 }
             }
-            if (GEOM == DD_GEOM_PARA) __syncwarp();
         }
+        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
-    // merge the two ownerships through shared memory
+    if (abort_flag) {
+        if (tid == 0) {
+            atomicExch(status, DD_ERR_TIMEOUT);
+            dd_mbar_wait(&bar[0], 0);
+            dd_mbar_wait(&bar[1], 0);
+        }
+        __syncthreads();
+        return;
+    }
+    // merge the two ownerships through shared memory (reusing the record buffers)
+    float (*tile)[kTile][kTile + 1] = reinterpret_cast<float (*)[kTile][kTile + 1]>(smem + SL.rec);
     for (int b = 0; b < nb; b++) {
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) tile[b][warp + kWarps * q][lane] = ax[q][b];
@@ -703,8 +859,7 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const float *bc = (const float *)(planb + P.bcoef);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    if (op == DD_OP_BPROJ_TW) return DD_ERR_UNSUPPORTED;   // see k_fwd_weighted (3-pass path)
-    auto kern = k_fwd<GEOM, 0>;
+    auto kern = (op == DD_OP_BPROJ_TW) ? k_fwd<GEOM, 1> : k_fwd<GEOM, 0>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
@@ -717,20 +872,19 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
 
 template <int GEOM>
 static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const char *planb,
-                      const float *angles, int B, int V, const float2 *dtab, float *out,
+                      const float *angles, int B, int V, const float2 *dtab, float *out, int *status,
                       cudaStream_t st) {
     dim3 grid((g->width + kTile - 1) / kTile, (g->height + kTile - 1) / kTile, (B + kBI - 1) / kBI);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
+    const AdjSmem S = adj_smem(GEOM);
+    auto kern = (op == DD_OP_PROJ_T) ? k_adj<GEOM, 0> : (op == DD_OP_BPROJ) ? k_adj<GEOM, 1> : k_adj<GEOM, 2>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
+        return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
-    if (op == DD_OP_PROJ_T)
-        k_adj<GEOM, 0><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
-    else if (op == DD_OP_BPROJ)
-        k_adj<GEOM, 1><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
-    else
-        k_adj<GEOM, 2><<<grid, kThreads, 0, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out);
+    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out, status);
     prof_end(pr, st);
     g_launches++;
     return launch_status();
@@ -772,9 +926,10 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
                                                      (const float *)(planb + P.dp),
                                                      (const float *)(planb + P.bcoef), pcx, pcy, dtab);
     prof_end(pr, st);
-    if (geom == DD_GEOM_PARA) return launch_adj<DD_GEOM_PARA>(op, g, P, planb, angles, B, V, dtab, out, st);
-    if (geom == DD_GEOM_FLAT) return launch_adj<DD_GEOM_FLAT>(op, g, P, planb, angles, B, V, dtab, out, st);
-    return launch_adj<DD_GEOM_ARC>(op, g, P, planb, angles, B, V, dtab, out, st);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
+    if (geom == DD_GEOM_PARA) return launch_adj<DD_GEOM_PARA>(op, g, P, planb, angles, B, V, dtab, out, status, st);
+    if (geom == DD_GEOM_FLAT) return launch_adj<DD_GEOM_FLAT>(op, g, P, planb, angles, B, V, dtab, out, status, st);
+    return launch_adj<DD_GEOM_ARC>(op, g, P, planb, angles, B, V, dtab, out, status, st);
 }
 
 }  // namespace dd2

@@ -27,23 +27,29 @@ from . import _native as N
 # ---------------------------------------------------------------------------
 # options on the host
 # ---------------------------------------------------------------------------
-_opt_cache: dict = {}
+_opt_cache: list = []   # (weakref(tensor), version, values) for device-resident options
 
 
 def host_options(options):
-    """Python floats of an options vector without re-reading device memory."""
+    """Python floats of an options vector without re-reading device memory.
+
+    Host tensors and sequences are read directly.  For a device tensor (the
+    reference moves projector.options to the GPU) the values are cached per
+    tensor object and version, so repeated calls do not synchronise.
+    """
+    import weakref
     if isinstance(options, (list, tuple)):
         return [float(x) for x in options]
     if not isinstance(options, torch.Tensor):
         raise RuntimeError("options must be a tensor or a sequence of numbers")
-    key = (options.data_ptr(), options._version, options.numel(), str(options.device))
-    hit = _opt_cache.get(key)
-    if hit is not None:
-        return hit
+    if options.device.type == "cpu":
+        return [float(x) for x in options.detach().double().reshape(-1).tolist()]
+    for ref, ver, vals in _opt_cache:
+        if ref() is options and ver == options._version:
+            return vals
     vals = [float(x) for x in options.detach().to("cpu", torch.float64).reshape(-1).tolist()]
-    if len(_opt_cache) > 256:
-        _opt_cache.clear()
-    _opt_cache[key] = vals
+    _opt_cache[:] = [e for e in _opt_cache if e[0]() is not None][-63:]
+    _opt_cache.append((weakref.ref(options), options._version, vals))
     return vals
 
 

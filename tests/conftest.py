@@ -58,7 +58,7 @@ class _G2(ctypes.Structure):
 
 class HostModel:
     """ctypes wrapper of tests/native/dd_model2d.cpp (host model of the kernels)."""
-    OPS = {"proj": 0, "proj_t": 1, "bproj": 2, "bproj_t": 3, "bproj_w": 4}
+    OPS = {"proj": 0, "proj_t": 1, "bproj": 2, "bproj_t": 3, "bproj_w": 4, "bproj_tw": 5}
     SCAN = {"para": 0, "flat": 1, "arc": 2}
 
     def __init__(self, path):
@@ -75,7 +75,7 @@ class HostModel:
         g = _G2(int(opt[0]), int(opt[1]), int(opt[2]), *[float(v) for v in opt[3:]])
         V = len(angles)
         B = x.shape[0]
-        shape = (B, V, int(opt[2])) if op in ("proj", "bproj_t") else (B, int(opt[1]), int(opt[0]))
+        shape = (B, V, int(opt[2])) if op in ("proj", "bproj_t", "bproj_tw") else (B, int(opt[1]), int(opt[0]))
         out = np.zeros(shape, np.float32)
         x = np.ascontiguousarray(x, np.float32)
         a = np.ascontiguousarray(angles, np.float32)

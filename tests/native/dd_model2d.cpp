@@ -82,14 +82,14 @@ int det_index_fan(int geom, const dd_geom2d &g, const DdView2 &vw, float view, f
 
 }  // namespace
 
-// op: 0 proj, 1 proj_t, 2 bproj, 3 bproj_t, 4 bproj_w.  scan: 0 para, 1 flat, 2 arc.
+// op: 0 proj, 1 proj_t, 2 bproj, 3 bproj_t, 4 bproj_w, 5 bproj_tw.  scan: 0 para, 1 flat, 2 arc.
 // in/out: reference layouts, batch B.  Returns 0 on success.
 extern "C" int model_apply2d(int scan, int op, const dd_geom2d *gp, const float *in, float *out,
                              const float *angles, int B, int V) {
     const dd_geom2d g = *gp;
     const int geom = scan;
     const int W = g.width, H = g.height, D = g.num_det;
-    const bool fwd = (op == 0 || op == 3);
+    const bool fwd = (op == 0 || op == 3 || op == 5);
     if (fwd) std::memset(out, 0, sizeof(float) * (size_t)B * V * D);
     else std::memset(out, 0, sizeof(float) * (size_t)B * H * W);
     std::vector<float> dp(D + 1), bc(D + 1);
@@ -133,8 +133,31 @@ extern "C" int model_apply2d(int scan, int op, const dd_geom2d *gp, const float 
                 const int idet0 = L.h.idet0;
                 if (fwd) {
                     const float *img = in + (size_t)b * H * W;
-                    const std::vector<F2> tab = vw.xb ? prefix(img + (size_t)line * W, W, 1)
-                                                      : prefix(img + (size_t)(H - 1) * W + line, H, -W);
+                    std::vector<F2> tab = vw.xb ? prefix(img + (size_t)line * W, W, 1)
+                                                : prefix(img + (size_t)(H - 1) * W + line, H, -W);
+                    if (op == 5) {
+                        // FBP-weighted transpose: weight every pixel at this view, rebuild the prefix
+                        const float lpos = vw.xb
+                            ? (float)(((double)H / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift)
+                            : (float)(((double)line - W / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
+                        float run = 0.0f;
+                        for (int i = 0; i < npix; i++) {
+                            float pcx, pcy;
+                            if (vw.xb) {
+                                pcx = (float)(((double)i + 0.5) * (double)g.pix_x + (double)vw.axis0);
+                                pcy = lpos;
+                            } else {
+                                pcx = lpos;
+                                pcy = (float)(((double)i + 0.5) * (double)g.pix_y + (double)vw.axis0);
+                            }
+                            const float w = (geom == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
+                                                                  : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                            const float y = tab[i].x * w;
+                            tab[i] = {run, y};
+                            run += y;
+                        }
+                        tab[npix] = {run, 0.0f};
+                    }
                     const std::vector<float> K = piece_K(L, tab.data());
                     const float scale = (op == 0) ? 1.0f : L.h.alpha;
                     float prev = 0.0f;

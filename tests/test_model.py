@@ -14,8 +14,8 @@ import pytest
 from conftest import rel_l2
 
 OPS = {"para": ["proj", "proj_t", "bproj", "bproj_t"],
-       "flat": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w"],
-       "arc": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w"]}
+       "flat": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"],
+       "arc": ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"]}
 
 
 def _cases():
@@ -29,7 +29,7 @@ def _cases():
 def test_model_matches_reference(golden, host_model, case, geom, op):
     opt = golden[f"{case}/options"]
     ang = golden[f"{case}/angles"]
-    x = golden[f"{case}/image"] if op in ("proj", "bproj_t") else golden[f"{case}/sino"]
+    x = golden[f"{case}/image"] if op in ("proj", "bproj_t", "bproj_tw") else golden[f"{case}/sino"]
     out = host_model.apply2d(geom, op, x, ang, opt)
     assert rel_l2(out, golden[f"{case}/{op}/ref"]) <= 1e-5
 
