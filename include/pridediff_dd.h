@@ -110,6 +110,55 @@ int dd2d_apply_planned(int scan, int op, const dd_geom2d *g, const void *plan, c
                        float *out, int batch, int num_view, void *workspace,
                        size_t workspace_bytes, dd_stream_t stream);
 
+/* ---- 2-D: data-consistency step -------------------------------------------
+ * x <- x - eta * A^T (A x - y) for a batch of slices sharing one geometry:
+ * the forward writes the residual A x - y into `resid` (B, V, D) directly and
+ * the exact adjoint updates x in place.  No counterpart in the reference: the
+ * PrideDiff caller builds it from two separate operator calls
+ * (model/pridediff.py:56-68).  `plan` from dd2d_plan; workspace size from
+ * dd2d_dc_workspace_bytes.  Capturable in a CUDA graph. */
+size_t dd2d_dc_workspace_bytes(int scan, const dd_geom2d *g, int batch, int num_view);
+int dd2d_dc_step(int scan, const dd_geom2d *g, const void *plan, float *x, const float *y, float *resid,
+                 float eta, int batch, int num_view, void *workspace, size_t workspace_bytes,
+                 dd_stream_t stream);
+
+/* ---- 2-D: uneven batches in one persistent launch --------------------------
+ * No counterpart in the reference, which runs one uniform geometry per call
+ * (batch folded into gridDim.x, ParaDisCUDA2d.cu:334-337).  An uneven batch
+ * is n instances of one scan type, each with its own geometry, view count and
+ * number of slices.  Inputs and outputs are packed instance after instance:
+ * images (batch_i, H_i, W_i), sinograms (batch_i, V_i, D_i).  Weighted
+ * operators are not batched. */
+typedef struct dd_instance2d {
+    dd_geom2d geom;
+    int num_view;
+    int batch;        /* slices sharing this geometry */
+} dd_instance2d;
+
+/* tuning of the persistent launches (chosen by the autotuner) */
+typedef struct dd_tune2d {
+    int ctas_per_sm;  /* persistent CTAs per SM (1..4; 0 = default 2) */
+    int lpt_order;    /* items longest-first (1) or in instance order (0) */
+    int reserved[6];
+} dd_tune2d;
+
+size_t dd2d_batch_plan_bytes(int scan, const dd_instance2d *inst, int n);
+size_t dd2d_batch_workspace_bytes(int scan, const dd_instance2d *inst, int n);
+/* Builds every instance's plan and the work lists.  angles[i] is the device
+ * pointer of instance i's angles.  Synchronises `stream` (plan time only). */
+int dd2d_batch_plan(int scan, const dd_instance2d *inst, int n, const float *const *angles, void *plan,
+                    size_t plan_bytes, const dd_tune2d *tune, dd_stream_t stream);
+int dd2d_batch_apply(int scan, int op, const dd_instance2d *inst, int n, const void *plan, const float *in,
+                     float *out, void *workspace, size_t workspace_bytes, const dd_tune2d *tune,
+                     dd_stream_t stream);
+/* x <- x - eta * A^T (A x - y) over all instances (packed x and y). */
+int dd2d_batch_dc_step(int scan, const dd_instance2d *inst, int n, const void *plan, float *x, const float *y,
+                       float eta, void *workspace, size_t workspace_bytes, const dd_tune2d *tune,
+                       dd_stream_t stream);
+/* Device status word of the last batched call (DD_OK or DD_ERR_TIMEOUT);
+ * synchronous. */
+int dd2d_batch_status(int scan, const dd_instance2d *inst, int n, const void *workspace, int *status);
+
 /* ---- 2-D: named entries, one per radontorch function --------------------
  * Same arguments as dd2d_apply without scan/op.  Each replaces the pybind
  * function of the same name (RadonTorch.cpp:1376-1393). */

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_BUILD, "libpridediff_dd.so")
 INCLUDE = os.path.join(_ROOT, "include")
 
 # translation units of the library (compiled in parallel)
-SOURCES = ["dd2d.cu"]
+SOURCES = ["dd2d.cu", "dd2d_batch.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -78,6 +78,14 @@ class _Geom2d(ctypes.Structure):
                                         "pix_xshift", "pix_yshift", "bin_shift")]
 
 
+class _Instance2d(ctypes.Structure):
+    _fields_ = [("geom", _Geom2d), ("num_view", ctypes.c_int), ("batch", ctypes.c_int)]
+
+
+class _Tune2d(ctypes.Structure):
+    _fields_ = [("ctas_per_sm", ctypes.c_int), ("lpt_order", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+
+
 class _Geom3d(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("width", "height", "depth", "num_col", "num_row")] + \
         [(n, ctypes.c_float) for n in ("pix_x", "pix_y", "pix_z", "col_size", "row_size",
@@ -87,6 +95,8 @@ class _Geom3d(ctypes.Structure):
 
 Geom2d = _Geom2d
 Geom3d = _Geom3d
+Instance2d = _Instance2d
+Tune2d = _Tune2d
 
 # status codes (include/pridediff_dd.h)
 DD_OK = 0
@@ -116,6 +126,24 @@ def _declare(lib):
     lib.dd2d_apply_workspace_bytes.argtypes = [i, i, g2, i, i]
     lib.dd2d_apply_planned.restype = i
     lib.dd2d_apply_planned.argtypes = [i, i, g2, vp, vp, vp, i, i, vp, sz, vp]
+    ip = ctypes.POINTER(_Instance2d)
+    tp = ctypes.POINTER(_Tune2d)
+    lib.dd2d_dc_workspace_bytes.restype = sz
+    lib.dd2d_dc_workspace_bytes.argtypes = [i, g2, i, i]
+    lib.dd2d_dc_step.restype = i
+    lib.dd2d_dc_step.argtypes = [i, g2, vp, vp, vp, vp, ctypes.c_float, i, i, vp, sz, vp]
+    lib.dd2d_batch_plan_bytes.restype = sz
+    lib.dd2d_batch_plan_bytes.argtypes = [i, ip, i]
+    lib.dd2d_batch_workspace_bytes.restype = sz
+    lib.dd2d_batch_workspace_bytes.argtypes = [i, ip, i]
+    lib.dd2d_batch_plan.restype = i
+    lib.dd2d_batch_plan.argtypes = [i, ip, i, ctypes.POINTER(ctypes.c_void_p), vp, sz, tp, vp]
+    lib.dd2d_batch_apply.restype = i
+    lib.dd2d_batch_apply.argtypes = [i, i, ip, i, vp, vp, vp, vp, sz, tp, vp]
+    lib.dd2d_batch_dc_step.restype = i
+    lib.dd2d_batch_dc_step.argtypes = [i, ip, i, vp, vp, vp, ctypes.c_float, vp, sz, tp, vp]
+    lib.dd2d_batch_status.restype = i
+    lib.dd2d_batch_status.argtypes = [i, ip, i, vp, ctypes.POINTER(ctypes.c_int)]
     lib.dd2d_validate.restype = i
     lib.dd2d_validate.argtypes = [i, i, g2, i, i]
     lib.dd_launch_count.restype = ctypes.c_ulonglong

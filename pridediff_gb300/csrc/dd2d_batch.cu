@@ -1,0 +1,501 @@
+// Batched 2-D DD projection over uneven instances in one persistent launch.
+//
+// An uneven batch is a list of instances, each with its own image size,
+// view count, detector count and number of slices (one scan type per batch).
+// The reference has no batching beyond folding the batch into gridDim.x with
+// one uniform geometry per call (ParaDisCUDA2d.cu:334-337); here every
+// instance's geometry plan lives in one plan buffer, the work of all
+// instances is cut into items (forward: one view x a group of slices;
+// adjoint: one 32x32 tile x a group of slices), and a persistent grid of
+// `ctas_per_sm` CTAs per SM pulls items from a device counter in
+// longest-first order.  The item bodies are the single-geometry ones
+// (dd2d_kernels.cuh), so results are identical to per-instance calls.
+//
+// The data-consistency step x <- x - eta * A^T (A x - y) is four launches:
+// image tables, forward items writing the residual A x - y directly, detector
+// tables of the residual, adjoint items updating x in place.  No host syncs,
+// no allocations: the step is capturable in a CUDA graph.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "dd2d_kernels.cuh"
+
+namespace dd2 {
+
+struct BatchInst {
+    dd_geom2d g;
+    int V, batch, nl, pad;
+    long long plan_off;            // bytes: instance plan inside the batch plan
+    long long img_off, sino_off;   // elements: packed images / sinograms
+    long long tabx_off, taby_off;  // float2: forward tables in the workspace
+    long long dtab_off;            // float2: adjoint tables in the workspace
+    long long views, ang, dp, bcoef, lines, dlines;   // PlanLayout offsets
+};
+
+struct BatchLayout {
+    size_t desc, fitems, aitems, plans, total;        // plan buffer
+    size_t w_tabs, w_dtab, w_resid, w_counter, w_status, w_total;   // workspace
+    int nfwd, nadj, Dmax, rsmax;
+    std::vector<BatchInst> inst;
+};
+
+static BatchLayout batch_layout(int scan, const dd_instance2d *in, int n, int bi) {
+    BatchLayout L;
+    L.inst.resize(n);
+    long long img = 0, sino = 0, tabs = 0, dtab = 0;
+    size_t plans = 0;
+    L.nfwd = L.nadj = 0;
+    L.Dmax = 1;
+    L.rsmax = 2;
+    for (int i = 0; i < n; i++) {
+        BatchInst &d = L.inst[i];
+        memset(&d, 0, sizeof(d));
+        d.g = in[i].geom;
+        d.V = in[i].num_view;
+        d.batch = in[i].batch;
+        const PlanLayout P = plan_layout(scan, &d.g, d.V);
+        d.nl = P.nl;
+        d.plan_off = (long long)plans;
+        plans = align_up(plans + P.total, 256);
+        d.views = (long long)P.views;
+        d.ang = (long long)P.ang;
+        d.dp = (long long)P.dp;
+        d.bcoef = (long long)P.bcoef;
+        d.lines = (long long)P.lines;
+        d.dlines = (long long)P.dlines;
+        const int W = d.g.width, H = d.g.height, D = d.g.num_det;
+        d.img_off = img;
+        img += (long long)d.batch * H * W;
+        d.sino_off = sino;
+        sino += (long long)d.batch * d.V * D;
+        d.tabx_off = tabs;
+        tabs += (long long)d.batch * H * rs_entries(W);
+        d.taby_off = tabs;
+        tabs += (long long)d.batch * W * rs_entries(H);
+        tabs = (tabs + 1) & ~1LL;
+        d.dtab_off = dtab;
+        dtab += ((long long)d.batch * d.V * rs_entries(D) + 1) & ~1LL;
+        const int groups = (d.batch + bi - 1) / bi;
+        L.nfwd += d.V * groups;
+        L.nadj += ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile) * groups;
+        L.Dmax = std::max(L.Dmax, D);
+        L.rsmax = std::max(L.rsmax, rs_entries(std::max(W, H)));
+    }
+    size_t o = 0;
+    L.desc = o; o = align_up(o + sizeof(BatchInst) * (size_t)n, 256);
+    L.fitems = o; o = align_up(o + sizeof(int4) * (size_t)L.nfwd, 256);
+    L.aitems = o; o = align_up(o + sizeof(int4) * (size_t)L.nadj, 256);
+    L.plans = o; o = align_up(o + plans, 256);
+    L.total = o;
+    size_t w = 0;
+    L.w_tabs = w; w = align_up(w + sizeof(float2) * (size_t)tabs, 256);
+    L.w_dtab = w; w = align_up(w + sizeof(float2) * (size_t)dtab, 256);
+    L.w_resid = w; w = align_up(w + sizeof(float) * (size_t)sino, 256);
+    L.w_counter = w; w = align_up(w + 2 * sizeof(int), 256);
+    L.w_status = w; w = align_up(w + sizeof(int), 256);
+    L.w_total = w;
+    return L;
+}
+
+// ---------------------------------------------------------------------------
+// Batched prefix tables (one launch each; blockIdx.y = instance)
+// ---------------------------------------------------------------------------
+__global__ void k_tab_rows_b(const BatchInst *__restrict__ desc, const float *__restrict__ img,
+                             float2 *__restrict__ tabs) {
+    const BatchInst &d = desc[blockIdx.y];
+    const int W = d.g.width, H = d.g.height;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= d.batch * H) return;
+    const float *row = img + d.img_off + (size_t)warp * W;
+    float2 *t = tabs + d.tabx_off + (size_t)warp * rs_entries(W);
+    double run = 0.0;
+    for (int j0 = 0; j0 <= W; j0 += 32) {
+        const int j = j0 + lane;
+        const float x = (j < W) ? row[j] : 0.0f;
+        double inc = (double)x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (j <= W) t[j] = make_float2((float)(run + inc - (double)x), x);
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+__global__ void k_tab_cols_b(const BatchInst *__restrict__ desc, const float *__restrict__ img,
+                             float2 *__restrict__ tabs) {
+    const BatchInst &d = desc[blockIdx.y];
+    const int W = d.g.width, H = d.g.height;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= d.batch * W) return;
+    const int b = idx / W, col = idx - b * W;
+    const float *im = img + d.img_off + (size_t)b * H * W;
+    float2 *t = tabs + d.taby_off + (size_t)idx * rs_entries(H);
+    double run = 0.0;
+    for (int i = 0; i < H; i++) {
+        const float x = im[(size_t)(H - 1 - i) * W + col];
+        t[i] = make_float2((float)run, x);
+        run += (double)x;
+    }
+    t[H] = make_float2((float)run, 0.0f);
+}
+
+__global__ void k_dettab_b(int geom, int mode, const BatchInst *__restrict__ desc,
+                           const char *__restrict__ plan, size_t plans_off,
+                           const float *__restrict__ sino, float2 *__restrict__ dtabs) {
+    const BatchInst &d = desc[blockIdx.y];
+    const int V = d.V, D = d.g.num_det;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= d.batch * V) return;
+    const int b = warp / V, v = warp - b * V;
+    const char *pb = plan + plans_off + d.plan_off;
+    const DdView2 vw = reinterpret_cast<const DdView2 *>(pb + d.views)[v];
+    const float *dpv = reinterpret_cast<const float *>(pb + d.dp) + (size_t)v * (D + 1);
+    const float *bc = reinterpret_cast<const float *>(pb + d.bcoef) + (size_t)v * (D + 1);
+    const float *s = sino + d.sino_off + ((size_t)b * V + v) * D;
+    float2 *t = dtabs + d.dtab_off + (size_t)warp * rs_entries(D);
+    const float pc = vw.xb ? d.g.pix_y / d.g.det_size : d.g.pix_x / d.g.det_size;
+    double run = 0.0;
+    for (int k0 = 0; k0 <= D; k0 += 32) {
+        const int k = k0 + lane;
+        float gk = 0.0f;
+        double w = 0.0;
+        if (k < D) {
+            const float sv = s[vw.flip ? D - 1 - k : k];
+            if (geom == DD_GEOM_PARA) {
+                gk = (mode == 0) ? sv * pc : sv;
+                w = 1.0;
+            } else {
+                gk = (mode == 0) ? sv * bc[k] : sv;
+                w = (double)(dpv[k + 1] - dpv[k]);
+            }
+        }
+        double inc = (double)gk * w;
+        const double mine = inc;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (k <= D) t[k] = make_float2((float)(run + inc - mine), gk);
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent item kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int next_item(int *counter) {
+    __shared__ int s_item;
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    __syncthreads();
+    return s_item;
+}
+
+template <int GEOM>
+__global__ void __launch_bounds__(kThreads)
+k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
+            const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
+            float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
+            int *__restrict__ counter, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax);
+    init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
+    uint32_t uses[2] = {0u, 0u};
+    for (;;) {
+        const int i = next_item(counter);
+        if (i >= nitems) break;
+        const int4 w = items[i];
+        const BatchInst &d = desc[w.x];
+        const char *pb = plan + plans_off + d.plan_off;
+        FwdItem it;
+        it.v = w.y;
+        it.b0 = w.z;
+        it.nb = w.w;
+        it.V = d.V;
+        it.nl = d.nl;
+        it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
+        it.dp = reinterpret_cast<const float *>(pb + d.dp);
+        it.bcoef = reinterpret_cast<const float *>(pb + d.bcoef);
+        it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
+        it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
+        it.tabx = tabs + d.tabx_off;
+        it.taby = tabs + d.taby_off;
+        it.out = out + d.sino_off;
+        it.sub = sub ? sub + d.sino_off : nullptr;
+        if (!fwd_view<GEOM, 0>(d.g, op, it, smem, Dmax, rsmax, uses)) {
+            if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+            break;
+        }
+    }
+}
+
+template <int GEOM, int OPK>
+__global__ void __launch_bounds__(kThreads)
+k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
+            const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ dtabs,
+            float *__restrict__ out, const float *__restrict__ base, float scale,
+            int *__restrict__ counter, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const AdjSmem SL = adj_smem(GEOM);
+    init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar));
+    uint32_t uses[2] = {0u, 0u};
+    for (;;) {
+        const int i = next_item(counter + 1);
+        if (i >= nitems) break;
+        const int4 w = items[i];
+        const BatchInst &d = desc[w.x];
+        const char *pb = plan + plans_off + d.plan_off;
+        AdjItem it;
+        it.c0 = (w.y & 0xFFFF) * kTile;
+        it.r0 = (w.y >> 16) * kTile;
+        it.b0 = w.z;
+        it.nb = w.w;
+        it.V = d.V;
+        it.nl = d.nl;
+        it.angles = reinterpret_cast<const float *>(pb + d.ang);
+        it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
+        it.dp = reinterpret_cast<const float *>(pb + d.dp);
+        it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
+        it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
+        it.dtab = dtabs + d.dtab_off;
+        it.out = out + d.img_off;
+        it.base = base ? base + d.img_off : nullptr;
+        it.scale = scale;
+        if (!adj_tile<GEOM, OPK>(d.g, it, smem, uses)) {
+            if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+            break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 1;
+    }
+    return n;
+}
+
+static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
+    if (!inst || n <= 0 || n > 65535) return DD_ERR_INVALID_ARG;
+    if (op == DD_OP_BPROJ_W || op == DD_OP_BPROJ_TW) return DD_ERR_UNSUPPORTED;
+    for (int i = 0; i < n; i++) {
+        const int st = validate(scan, op, &inst[i].geom, inst[i].batch, inst[i].num_view);
+        if (st != DD_OK) return st;
+        if ((inst[i].geom.width + kTile - 1) / kTile > 0xFFFF) return DD_ERR_SIZE_OVERFLOW;
+    }
+    return DD_OK;
+}
+
+template <int GEOM>
+static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
+                            float *out, const float *sub, int *counter, int *status, int grid,
+                            cudaStream_t st) {
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax);
+    auto kern = k_fwd_items<GEOM>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
+    kern<<<grid, kThreads, S.total, st>>>(op, (const BatchInst *)(planb + L.desc),
+                                          (const int4 *)(planb + L.fitems), L.nfwd, planb, L.plans, tabs,
+                                          out, sub, L.Dmax, L.rsmax, counter, status);
+    prof_end(pr, st);
+    count_launches(1);
+    return launch_status();
+}
+
+template <int GEOM>
+static int launch_adj_items(int op, const BatchLayout &L, const char *planb, const float2 *dtabs,
+                            float *out, const float *base, float scale, int *counter, int *status,
+                            int grid, cudaStream_t st) {
+    const AdjSmem S = adj_smem(GEOM);
+    auto kern = (op == DD_OP_PROJ_T) ? k_adj_items<GEOM, 0> : k_adj_items<GEOM, 1>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
+    kern<<<grid, kThreads, S.total, st>>>((const BatchInst *)(planb + L.desc),
+                                          (const int4 *)(planb + L.aitems), L.nadj, planb, L.plans, dtabs,
+                                          out, base, scale, counter, status);
+    prof_end(pr, st);
+    count_launches(1);
+    return launch_status();
+}
+
+static int grid_of(const dd_tune2d *t, int nitems) {
+    int per = (t && t->ctas_per_sm > 0) ? t->ctas_per_sm : 2;
+    if (per > 4) per = 4;
+    return std::max(1, std::min(nitems, per * sm_count()));
+}
+
+// forward of all instances: out = A in (- sub)
+static int batch_forward(int scan, int op, const BatchLayout &L, const char *planb, const float *in,
+                         float *out, const float *sub, char *wb, const dd_tune2d *tune, cudaStream_t st) {
+    const int geom = geom_of(scan);
+    float2 *tabs = (float2 *)(wb + L.w_tabs);
+    int *counter = (int *)(wb + L.w_counter);
+    int *status = (int *)(wb + L.w_status);
+    const BatchInst *desc = (const BatchInst *)(planb + L.desc);
+    int maxrows = 1, maxcols = 1;
+    for (const BatchInst &d : L.inst) {
+        maxrows = std::max(maxrows, d.batch * d.g.height);
+        maxcols = std::max(maxcols, d.batch * d.g.width);
+    }
+    const int n = (int)L.inst.size();
+    ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
+    k_tab_rows_b<<<dim3((maxrows * 32 + 255) / 256, n), 256, 0, st>>>(desc, in, tabs);
+    k_tab_cols_b<<<dim3((maxcols + 127) / 128, n), 128, 0, st>>>(desc, in, tabs);
+    prof_end(pr, st);
+    count_launches(2);
+    if (cudaMemsetAsync(counter, 0, 2 * sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
+    const int grid = grid_of(tune, L.nfwd);
+    if (geom == DD_GEOM_PARA) return launch_fwd_items<DD_GEOM_PARA>(op, L, planb, tabs, out, sub, counter, status, grid, st);
+    if (geom == DD_GEOM_FLAT) return launch_fwd_items<DD_GEOM_FLAT>(op, L, planb, tabs, out, sub, counter, status, grid, st);
+    return launch_fwd_items<DD_GEOM_ARC>(op, L, planb, tabs, out, sub, counter, status, grid, st);
+}
+
+// adjoint of all instances: out = base + scale * (A^T in)   (base may be null)
+static int batch_adjoint(int scan, int op, const BatchLayout &L, const char *planb, const float *in,
+                         float *out, const float *base, float scale, char *wb, const dd_tune2d *tune,
+                         cudaStream_t st) {
+    const int geom = geom_of(scan);
+    float2 *dtabs = (float2 *)(wb + L.w_dtab);
+    int *counter = (int *)(wb + L.w_counter);
+    int *status = (int *)(wb + L.w_status);
+    const BatchInst *desc = (const BatchInst *)(planb + L.desc);
+    int maxw = 1;
+    for (const BatchInst &d : L.inst) maxw = std::max(maxw, d.batch * d.V);
+    const int n = (int)L.inst.size();
+    ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
+    k_dettab_b<<<dim3((maxw * 32 + 255) / 256, n), 256, 0, st>>>(geom, op == DD_OP_PROJ_T ? 0 : 1, desc,
+                                                                  planb, L.plans, in, dtabs);
+    prof_end(pr, st);
+    count_launches(1);
+    if (cudaMemsetAsync(counter, 0, 2 * sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
+    const int grid = grid_of(tune, L.nadj);
+    if (geom == DD_GEOM_PARA) return launch_adj_items<DD_GEOM_PARA>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
+    if (geom == DD_GEOM_FLAT) return launch_adj_items<DD_GEOM_FLAT>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
+    return launch_adj_items<DD_GEOM_ARC>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
+}
+
+}  // namespace dd2
+
+using namespace dd2;
+
+extern "C" size_t dd2d_batch_plan_bytes(int scan, const dd_instance2d *inst, int n) {
+    if (validate_batch(scan, DD_OP_PROJ, inst, n) != DD_OK) return 0;
+    return batch_layout(scan, inst, n, kBI).total;
+}
+
+extern "C" size_t dd2d_batch_workspace_bytes(int scan, const dd_instance2d *inst, int n) {
+    if (validate_batch(scan, DD_OP_PROJ, inst, n) != DD_OK) return 0;
+    return batch_layout(scan, inst, n, kBI).w_total;
+}
+
+extern "C" int dd2d_batch_plan(int scan, const dd_instance2d *inst, int n, const float *const *angles,
+                               void *planp, size_t plan_bytes, const dd_tune2d *tune, dd_stream_t stream) {
+    const int vs = validate_batch(scan, DD_OP_PROJ, inst, n);
+    if (vs != DD_OK) return vs;
+    if (!angles || !planp) return DD_ERR_INVALID_ARG;
+    for (int i = 0; i < n; i++)
+        if (!angles[i]) return DD_ERR_INVALID_ARG;
+    BatchLayout L = batch_layout(scan, inst, n, kBI);
+    if (plan_bytes < L.total) return DD_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *pb = (char *)planp;
+    // work items; longest first unless the tuning asks for instance order
+    struct Item {
+        int4 w;
+        long long cost;
+    };
+    std::vector<Item> fw, aw;
+    fw.reserve(L.nfwd);
+    aw.reserve(L.nadj);
+    for (int i = 0; i < n; i++) {
+        const BatchInst &d = L.inst[i];
+        const int W = d.g.width, H = d.g.height, D = d.g.num_det;
+        for (int b0 = 0; b0 < d.batch; b0 += kBI) {
+            const int nb = std::min(kBI, d.batch - b0);
+            for (int v = 0; v < d.V; v++)
+                fw.push_back({make_int4(i, v, b0, nb), (long long)std::max(W, H) * (D + 1) * nb});
+            for (int ty = 0; ty < (H + kTile - 1) / kTile; ty++)
+                for (int tx = 0; tx < (W + kTile - 1) / kTile; tx++)
+                    aw.push_back({make_int4(i, tx | (ty << 16), b0, nb), (long long)d.V * nb});
+        }
+    }
+    const bool lpt = !tune || tune->lpt_order != 0;
+    if (lpt) {
+        std::stable_sort(fw.begin(), fw.end(), [](const Item &a, const Item &b) { return a.cost > b.cost; });
+        std::stable_sort(aw.begin(), aw.end(), [](const Item &a, const Item &b) { return a.cost > b.cost; });
+    }
+    std::vector<int4> fi(fw.size()), ai(aw.size());
+    for (size_t k = 0; k < fw.size(); k++) fi[k] = fw[k].w;
+    for (size_t k = 0; k < aw.size(); k++) ai[k] = aw[k].w;
+    // descriptors and item lists (plan time only: synchronous copies)
+    if (cudaMemcpyAsync(pb + L.desc, L.inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(pb + L.fitems, fi.data(), sizeof(int4) * fi.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(pb + L.aitems, ai.data(), sizeof(int4) * ai.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    for (int i = 0; i < n; i++) {
+        const BatchInst &d = L.inst[i];
+        const int s2 = plan(scan, &d.g, angles[i], d.V, pb + L.plans + d.plan_off,
+                            plan_layout(scan, &d.g, d.V).total, st);
+        if (s2 != DD_OK) return s2;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return DD_ERR_LAUNCH;
+    return DD_OK;
+}
+
+extern "C" int dd2d_batch_apply(int scan, int op, const dd_instance2d *inst, int n, const void *planp,
+                                const float *in, float *out, void *ws, size_t wsb, const dd_tune2d *tune,
+                                dd_stream_t stream) {
+    const int vs = validate_batch(scan, op, inst, n);
+    if (vs != DD_OK) return vs;
+    if (!planp || !in || !out) return DD_ERR_INVALID_ARG;
+    const BatchLayout L = batch_layout(scan, inst, n, kBI);
+    if (!ws || wsb < L.w_total) return DD_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *wb = (char *)ws;
+    if (cudaMemsetAsync(wb + L.w_status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
+    if (op_is_forward(op))
+        return batch_forward(scan, op, L, (const char *)planp, in, out, nullptr, wb, tune, st);
+    return batch_adjoint(scan, op, L, (const char *)planp, in, out, nullptr, 1.0f, wb, tune, st);
+}
+
+extern "C" int dd2d_batch_dc_step(int scan, const dd_instance2d *inst, int n, const void *planp, float *x,
+                                  const float *y, float eta, void *ws, size_t wsb, const dd_tune2d *tune,
+                                  dd_stream_t stream) {
+    const int vs = validate_batch(scan, DD_OP_PROJ, inst, n);
+    if (vs != DD_OK) return vs;
+    if (!planp || !x || !y) return DD_ERR_INVALID_ARG;
+    const BatchLayout L = batch_layout(scan, inst, n, kBI);
+    if (!ws || wsb < L.w_total) return DD_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *wb = (char *)ws;
+    float *resid = (float *)(wb + L.w_resid);
+    const char *pb = (const char *)planp;
+    if (cudaMemsetAsync(wb + L.w_status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
+    int s1 = batch_forward(scan, DD_OP_PROJ, L, pb, x, resid, y, wb, tune, st);
+    if (s1 != DD_OK) return s1;
+    return batch_adjoint(scan, DD_OP_PROJ_T, L, pb, resid, x, x, -eta, wb, tune, st);
+}
+
+extern "C" int dd2d_batch_status(int scan, const dd_instance2d *inst, int n, const void *ws, int *status) {
+    if (validate_batch(scan, DD_OP_PROJ, inst, n) != DD_OK || !ws || !status) return DD_ERR_INVALID_ARG;
+    const BatchLayout L = batch_layout(scan, inst, n, kBI);
+    if (cudaMemcpy(status, (const char *)ws + L.w_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    return DD_OK;
+}
