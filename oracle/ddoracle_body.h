@@ -346,6 +346,7 @@ typedef struct {
     T sdd, iso;            /* (spiral-corrected) distances                  */
     T axial;               /* spiral: table axial source position          */
     T detcol0xy;           /* flat: x (y) of virtual column boundary 0      */
+    T vds, vbs;            /* flat: virtual column pitch / shift            */
     T di;                  /* flat: column pitch projected on the axis      */
     T bp_scale;            /* DD-BP per-bin scale: VirDetColSize / DetColRad */
     T *dp;                 /* C+1 sorted column boundaries on the axis       */
@@ -365,6 +366,7 @@ static void FN(setup_view3)(const ddo_geom3 *g, int geom, T view, const float *s
     w->di = 0;
     w->detcol0xy = 0;
     w->axial = 0;
+    w->vds = w->vbs = 0;
     w->iso = R;
     w->sdd = SDD;
     w->srcz = 0;
@@ -409,6 +411,8 @@ static void FN(setup_view3)(const ddo_geom3 *g, int geom, T view, const float *s
         }
         w->di = vds * (T)fabs((double)(w->xb ? c : s));
         w->bp_scale = vds;
+        w->vds = vds;
+        w->vbs = vbs;
     } else {
         /* arc / spiral: ConeArcDisCUDA3d.cu:49-60 */
         for (int k = 0; k <= C; k++) {
@@ -507,15 +511,22 @@ static void FN(walk_row3)(const ddo_geom3 *g, int geom, int op, int v, int r,
         const T pint = (p1 - p0) / (T)npix;
         const T pintz = (p1z - p0z) / (T)Dp;
         const T parea = pint * pintz;
+        /* the reference walks each block of 256 detector columns separately
+         * (ConeFlatDisCUDA3d.cu:53-56, :116-130): every block restarts the
+         * walk, and with it the FP32 accumulation of the pixel boundaries */
+        for (int c0 = 0; c0 < C; c0 += 256) {
+        const int maxn = (C - c0 < 256) ? C - c0 : 256;
         int ipix, idet;
         T bound0;
         if (geom == DDO_CONE_FLAT) {
-            bound0 = p0 > w->dp[0] ? p0 : w->dp[0];
+            bound0 = p0 > w->dp[c0] ? p0 : w->dp[c0];
             if (p0 == bound0) {
                 T back = xb ? w->srcy * bound0 / ((bound0 - w->srcx) * w->s / w->c + w->srcy)
                             : w->srcx * bound0 / ((bound0 - w->srcy) * w->c / w->s + w->srcx);
+                const double uc = w->flip ? (C / 2.0 - c0) * w->vds + w->vbs : (c0 - C / 2.0) * w->vds + w->vbs;
+                const T col0 = xb ? (T)(uc * (double)w->c) : (T)(uc * (double)w->s);
                 ipix = 0;
-                idet = (int)floor((double)((back - w->detcol0xy) / w->di));
+                idet = (int)floor((double)((back - col0) / w->di));
             } else {
                 ipix = (int)floor((double)((bound0 - p0) / pint));
                 idet = 0;
@@ -532,9 +543,9 @@ static void FN(walk_row3)(const ddo_geom3 *g, int geom, int op, int v, int r,
                 tan1 = -1 / (T)tan((double)base);
             }
             T delta = (T)atan((double)((tan0 - tan1) / (1 + tan0 * tan1)));
-            idet = (int)floor(C / 2.0 + delta * (T)w->flag / w->colsz);
+            idet = (int)floor(C / 2.0 - c0 + delta * (T)w->flag / w->colsz);
             if (idet < 0) {
-                bound0 = w->dp[0];
+                bound0 = w->dp[c0];
                 ipix = (int)floor((double)((bound0 - p0) / pint));
                 idet = 0;
             } else {
@@ -544,12 +555,13 @@ static void FN(walk_row3)(const ddo_geom3 *g, int geom, int op, int v, int r,
         }
         if (idet < 0) idet = 0;
         T point1 = (T)(ipix + 1) * pint + p0;
-        T det1 = (idet < C) ? w->dp[idet + 1] : 0;
+        T det1 = (idet < maxn) ? w->dp[c0 + idet + 1] : 0;
         T pcx = xb ? (T)((ipix + 0.5) * sx + axis0) : lpos;
         T pcy = xb ? lpos : (T)((ipix + 0.5) * sy + axis0);
-        while (ipix < npix && idet < C) {
-            T bz0 = p0z > rp0[idet] ? p0z : rp0[idet];
-            const T bz1 = p1z < rp1[idet] ? p1z : rp1[idet];
+        while (ipix < npix && idet < maxn) {
+            const int col = c0 + idet;
+            T bz0 = p0z > rp0[col] ? p0z : rp0[col];
+            const T bz1 = p1z < rp1[col] ? p1z : rp1[col];
             int islice = (bz0 == p0z) ? 0 : (int)floor((double)((bz0 - p0z) / pintz));
             T pz1 = (T)(islice + 1) * pintz + p0z;
             const int step_pix = (point1 < det1);
@@ -563,16 +575,16 @@ static void FN(walk_row3)(const ddo_geom3 *g, int geom, int op, int v, int r,
             }
             const int lrow = xb ? line : H - 1 - ipix;
             const int lcol = xb ? ipix : line;
-            const long long detidx = ((long long)v * Rn + r) * C + (w->flip ? C - 1 - idet : idet);
+            const long long detidx = ((long long)v * Rn + r) * C + (w->flip ? C - 1 - col : col);
             while (bz0 < bz1 && islice < Dp) {
                 pz1 = (pz1 > bz1) ? bz1 : pz1;
                 const long long vox = ((long long)islice * H + lrow) * W + lcol;
                 const T zc = (pz1 - bz0) * coef;
                 for (int b = 0; b < batch; b++) {
                     if (proj_type) {
-                        binacc[b * C + idet] += zc * in[b * vox_b + vox];
+                        binacc[b * C + col] += zc * in[b * vox_b + vox];
                     } else {
-                        const T val = zc * (in[b * det_b + detidx] * scale[idet]);
+                        const T val = zc * (in[b * det_b + detidx] * scale[col]);
                         if (atomic) FN(atomic_add)(out + b * vox_b + vox, val);
                         else out[b * vox_b + vox] += val;
                     }
@@ -589,8 +601,9 @@ static void FN(walk_row3)(const ddo_geom3 *g, int geom, int op, int v, int r,
             } else {
                 bound0 = det1;
                 idet++;
-                if (idet < C) det1 = w->dp[idet + 1];
+                if (idet < maxn) det1 = w->dp[c0 + idet + 1];
             }
+        }
         }
     }
     if (proj_type) {
