@@ -184,6 +184,19 @@ DD_NAMED2D(BackProjParaDis2d);              /* RadonTorch.cpp:502  */
 DD_NAMED2D(BackProjTransParaDis2d);         /* RadonTorch.cpp:536  */
 #undef DD_NAMED2D
 
+/* ---- 2-D: forward projection without any caller workspace ----------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (a plugin whose host framework owns all device memory, a real-time
+ * loop that may not touch the allocator): same computation as
+ * dd_ProjFanFlatDis2d, with its scratch taken from a 32 MiB buffer that is
+ * part of the library (kept on every GPU that loads the library until the
+ * process exits).  Problems needing more scratch than that
+ * (dd2d_workspace_bytes) are refused with DD_ERR_WORKSPACE.  The first call
+ * on a device resolves the buffer's address; make it before any stream
+ * capture.  Calls share the buffer: calls that overlap on the GPU race. */
+int dd_ProjFanFlatDis2d_noalloc(const dd_geom2d *g, const float *in, float *out, const float *angles,
+                                int batch, int num_view, dd_stream_t stream);
+
 /* ---- diagnostics ----------------------------------------------------------
  * No counterpart in the reference (it has no instrumentation).  Kernel kinds
  * for dd_profile_read: */

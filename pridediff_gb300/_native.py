@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_BUILD, "libpridediff_dd.so")
 INCLUDE = os.path.join(_ROOT, "include")
 
 # translation units of the library (compiled in parallel)
-SOURCES = ["dd2d.cu", "dd2d_batch.cu"]
+SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd2d_noalloc.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
