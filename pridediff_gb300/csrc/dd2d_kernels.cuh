@@ -331,8 +331,10 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             const int ko = vw.flip ? D - 1 - k : k;
             for (int b = 0; b < nb; b++) {
                 const size_t o = ((size_t)(b0 + b) * it.V + v) * D + ko;
-                float val = acc[m][b] * beta;
-                if (it.sub) val -= it.sub[o];
+                // rounded product, then rounded difference: bit-equal to a
+                // separate projection followed by a subtraction (no FMA)
+                float val = __fmul_rn(acc[m][b], beta);
+                if (it.sub) val = __fsub_rn(val, it.sub[o]);
                 it.out[o] = val;
             }
         }
