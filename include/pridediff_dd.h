@@ -184,6 +184,55 @@ DD_NAMED2D(BackProjParaDis2d);              /* RadonTorch.cpp:502  */
 DD_NAMED2D(BackProjTransParaDis2d);         /* RadonTorch.cpp:536  */
 #undef DD_NAMED2D
 
+/* ---- 3-D: cone-flat, cone-arc, spiral --------------------------------------
+ * Same conventions as 2-D.  source_pos is the spiral source table (4, V) on
+ * the device (RadonTorch.cpp:1040-1043); pass NULL for the cone geometries.
+ * The reference has no CPU path for 3-D (RadonTorch.cpp:604). */
+int dd3d_validate(int scan, int op, const dd_geom3d *g, int batch, int num_view);
+size_t dd3d_workspace_bytes(int scan, int op, const dd_geom3d *g, int batch, int num_view);
+int dd3d_apply(int scan, int op, const dd_geom3d *g, const float *in, float *out, const float *angles,
+               const float *source_pos, int batch, int num_view, void *workspace, size_t workspace_bytes,
+               dd_stream_t stream);
+/* plan reuse: per-view column / row tables and the per-(view, line, 256-column
+ * block) drift records (the reference restarts its FP32 walk per block,
+ * ConeFlatDisCUDA3d.cu:53-56) */
+size_t dd3d_plan_bytes(int scan, const dd_geom3d *g, int num_view);
+int dd3d_plan(int scan, const dd_geom3d *g, const float *angles, const float *source_pos, int num_view,
+              void *plan, size_t plan_bytes, dd_stream_t stream);
+size_t dd3d_apply_workspace_bytes(int scan, int op, const dd_geom3d *g, int batch, int num_view);
+int dd3d_apply_planned(int scan, int op, const dd_geom3d *g, const void *plan, const float *in, float *out,
+                       int batch, int num_view, void *workspace, size_t workspace_bytes, dd_stream_t stream);
+/* x <- x - eta * A^T (A x - y) (no counterpart in the reference; the PrideDiff
+ * caller composes two operator calls, model/pridediff.py:56-68) */
+size_t dd3d_dc_workspace_bytes(int scan, const dd_geom3d *g, int batch, int num_view);
+int dd3d_dc_step(int scan, const dd_geom3d *g, const void *plan, float *x, const float *y, float *resid,
+                 float eta, int batch, int num_view, void *workspace, size_t workspace_bytes, dd_stream_t stream);
+
+/* named entries, one per 3-D radontorch function (RadonTorch.cpp:1395-1414) */
+#define DD_NAMED3D(name)                                                                          \
+    int dd_##name(const dd_geom3d *g, const float *in, float *out, const float *angles,           \
+                  const float *source_pos, int batch, int num_view, void *workspace,              \
+                  size_t workspace_bytes, dd_stream_t stream)
+DD_NAMED3D(ProjConeFlatDis3d);                  /* RadonTorch.cpp:572  */
+DD_NAMED3D(ProjTransConeFlatDis3d);             /* RadonTorch.cpp:609  */
+DD_NAMED3D(BackProjConeFlatDis3d);              /* RadonTorch.cpp:646  */
+DD_NAMED3D(BackProjTransConeFlatDis3d);         /* RadonTorch.cpp:683  */
+DD_NAMED3D(BackProjWeightedConeFlatDis3d);      /* RadonTorch.cpp:720  */
+DD_NAMED3D(BackProjTransWeightedConeFlatDis3d); /* RadonTorch.cpp:757  */
+DD_NAMED3D(ProjConeArcDis3d);                   /* RadonTorch.cpp:795  */
+DD_NAMED3D(ProjTransConeArcDis3d);              /* RadonTorch.cpp:832  */
+DD_NAMED3D(BackProjConeArcDis3d);               /* RadonTorch.cpp:869  */
+DD_NAMED3D(BackProjTransConeArcDis3d);          /* RadonTorch.cpp:906  */
+DD_NAMED3D(BackProjWeightedConeArcDis3d);       /* RadonTorch.cpp:943  */
+DD_NAMED3D(BackProjTransWeightedConeArcDis3d);  /* RadonTorch.cpp:980  */
+DD_NAMED3D(ProjSpiralDis3d);                    /* RadonTorch.cpp:1018 */
+DD_NAMED3D(ProjTransSpiralDis3d);               /* RadonTorch.cpp:1060 */
+DD_NAMED3D(BackProjSpiralDis3d);                /* RadonTorch.cpp:1102 */
+DD_NAMED3D(BackProjTransSpiralDis3d);           /* RadonTorch.cpp:1144 */
+DD_NAMED3D(BackProjWeightedSpiralDis3d);        /* RadonTorch.cpp:1186 */
+DD_NAMED3D(BackProjTransWeightedSpiralDis3d);   /* RadonTorch.cpp:1228 */
+#undef DD_NAMED3D
+
 /* ---- 2-D: forward projection without any caller workspace ----------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a plugin whose host framework owns all device memory, a real-time

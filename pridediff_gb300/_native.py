@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_BUILD, "libpridediff_dd.so")
 INCLUDE = os.path.join(_ROOT, "include")
 
 # translation units of the library (compiled in parallel)
-SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd2d_noalloc.cu"]
+SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd3d.cu", "dd2d_noalloc.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -108,6 +108,7 @@ DD_ERR_TIMEOUT = 5
 DD_ERR_UNSUPPORTED = 6
 
 SCAN2D = {"para": 0, "flat": 1, "arc": 2}
+SCAN3D = {"cone_flat": 0, "cone_arc": 1, "spiral": 2}
 OPS = {"proj": 0, "proj_t": 1, "bproj": 2, "bproj_t": 3, "bproj_w": 4, "bproj_tw": 5}
 
 
@@ -146,6 +147,25 @@ def _declare(lib):
     lib.dd2d_batch_status.argtypes = [i, ip, i, vp, ctypes.POINTER(ctypes.c_int)]
     lib.dd2d_validate.restype = i
     lib.dd2d_validate.argtypes = [i, i, g2, i, i]
+    g3 = ctypes.POINTER(_Geom3d)
+    lib.dd3d_validate.restype = i
+    lib.dd3d_validate.argtypes = [i, i, g3, i, i]
+    lib.dd3d_workspace_bytes.restype = sz
+    lib.dd3d_workspace_bytes.argtypes = [i, i, g3, i, i]
+    lib.dd3d_apply.restype = i
+    lib.dd3d_apply.argtypes = [i, i, g3, vp, vp, vp, vp, i, i, vp, sz, vp]
+    lib.dd3d_plan_bytes.restype = sz
+    lib.dd3d_plan_bytes.argtypes = [i, g3, i]
+    lib.dd3d_plan.restype = i
+    lib.dd3d_plan.argtypes = [i, g3, vp, vp, i, vp, sz, vp]
+    lib.dd3d_apply_workspace_bytes.restype = sz
+    lib.dd3d_apply_workspace_bytes.argtypes = [i, i, g3, i, i]
+    lib.dd3d_apply_planned.restype = i
+    lib.dd3d_apply_planned.argtypes = [i, i, g3, vp, vp, vp, i, i, vp, sz, vp]
+    lib.dd3d_dc_workspace_bytes.restype = sz
+    lib.dd3d_dc_workspace_bytes.argtypes = [i, g3, i, i]
+    lib.dd3d_dc_step.restype = i
+    lib.dd3d_dc_step.argtypes = [i, g3, vp, vp, vp, vp, ctypes.c_float, i, i, vp, sz, vp]
     lib.dd_launch_count.restype = ctypes.c_ulonglong
     lib.dd_launch_count.argtypes = []
     lib.dd_profile_enable.restype = i

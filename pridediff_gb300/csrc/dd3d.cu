@@ -1,0 +1,712 @@
+// 3-D DD projector (cone-flat, cone-arc, spiral): plan kernels, the
+// forward-type kernel (detector gathers) and the adjoint-type kernel (voxel
+// gathers), and the C ABI of include/pridediff_dd.h for the 18 3-D
+// radontorch operators (RadonTorch.cpp:1395-1414).
+//
+// Forward-type operators (Proj, BackProjTrans, BackProjTransWeighted): one
+// thread per (view, column, 8 detector rows, 2 volumes) loops over the walked
+// image lines; for each line it enumerates the overlap segments of its
+// column with the drifted pixel boundaries (dd3_colwalk_*), then walks the
+// slices each of its rows meets and gathers voxels.  Volumes are read from a
+// transposed copy for views that walk image columns, so that the pixels of a
+// walked line are contiguous in both branches.
+//
+// Adjoint-type operators (ProjTrans, BackProj, BackProjWeighted): one thread
+// per (x, y) voxel column, 8 slices and 2 volumes loops over the views; for
+// each view it enumerates the segments of its pixel with the detector columns
+// (dd3_pixwalk_*) and gathers the rows that meet each slice from a sinogram
+// pre-multiplied by the per-bin scale.  A per-CTA test skips views whose
+// detector cannot see the CTA's slab (most views of a spiral scan).
+//
+// Both directions use the same segment widths and z-walk widths, so they are
+// exact transposes of each other; no atomics, deterministic results.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pridediff_dd.h"
+#include "dd_geom3d.cuh"
+
+namespace dd2 {   // launch accounting and profiling (dd2d.cu)
+struct ProfRec;
+ProfRec *prof_begin(int kind, cudaStream_t st);
+void prof_end(ProfRec *r, cudaStream_t st);
+void count_launches(int n);
+}   // namespace dd2
+
+namespace dd3 {
+
+constexpr int kThreads = 256;
+constexpr int kRB = 8;     // detector rows per forward thread
+constexpr int kNB = 2;     // volumes per thread
+constexpr int kNS = 4;     // column segments held in registers per pass
+constexpr int kTile = 16;  // adjoint: 16 x 16 voxel columns per CTA
+constexpr int kZS = 8;     // adjoint: slices per thread
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// Layouts
+// ---------------------------------------------------------------------------
+struct PlanLayout {
+    size_t views, dp, mag, rowz, linez, lines, total;
+    int nl, nch;
+};
+
+inline PlanLayout plan_layout(const dd_geom3d *g, int V) {
+    PlanLayout L;
+    const int C = g->num_col, R = g->num_row;
+    L.nl = g->height > g->width ? g->height : g->width;
+    L.nch = (C + DD3_CHUNK - 1) / DD3_CHUNK;
+    size_t o = 0;
+    L.views = o; o = align_up(o + sizeof(DdView3) * (size_t)V, 256);
+    L.dp = o; o = align_up(o + sizeof(float) * (size_t)V * (C + 1), 256);
+    L.mag = o; o = align_up(o + sizeof(float) * (size_t)V * C, 256);
+    L.rowz = o; o = align_up(o + sizeof(float) * 2 * (size_t)V * R, 256);
+    L.linez = o; o = align_up(o + sizeof(float4) * (size_t)V * L.nl, 256);
+    L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl * L.nch, 256);
+    L.total = o;
+    return L;
+}
+
+struct ApplyLayout {
+    size_t volT, ss, status, total;
+};
+
+inline bool op_is_forward(int op) { return op == DD_OP_PROJ || op == DD_OP_BPROJ_T || op == DD_OP_BPROJ_TW; }
+inline int op_family(int op) {
+    return (op == DD_OP_PROJ || op == DD_OP_PROJ_T) ? 0 : (op == DD_OP_BPROJ_W || op == DD_OP_BPROJ_TW) ? 2 : 1;
+}
+
+// fwd / adj select which scratch areas are needed (both for the DC step)
+inline ApplyLayout apply_layout(bool fwd, bool adj, const dd_geom3d *g, int B, int V) {
+    ApplyLayout L;
+    size_t o = 0;
+    L.volT = L.ss = 0;
+    if (fwd) { L.volT = o; o = align_up(o + sizeof(float) * (size_t)B * g->depth * g->width * g->height, 256); }
+    if (adj) { L.ss = o; o = align_up(o + sizeof(float) * (size_t)B * V * g->num_row * g->num_col, 256); }
+    L.status = o; o = align_up(o + 256, 256);
+    L.total = o;
+    return L;
+}
+
+// ---------------------------------------------------------------------------
+// Plan kernels
+// ---------------------------------------------------------------------------
+// One CTA per view: scalars, column boundaries, column magnifications, row
+// table, and the ranges used by the adjoint's candidate searches.
+template <int GEOM>
+__global__ void __launch_bounds__(kThreads) k_views3(dd_geom3d g, const float *__restrict__ angles,
+                                                     const float *__restrict__ sp, int V, char *plan,
+                                                     PlanLayout P) {
+    const int v = blockIdx.x, tid = threadIdx.x;
+    const int C = g.num_col, R = g.num_row;
+    __shared__ DdView3 sw;
+    __shared__ float red[2][kThreads / 32];
+    if (tid == 0) {
+        float sp4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (GEOM == DD_GEOM3_SPIRAL)
+            for (int i = 0; i < 4; i++) sp4[i] = sp[(size_t)i * V + v];
+        dd3_view_scalars(GEOM, &g, angles[v], sp4, &sw);
+    }
+    __syncthreads();
+    const DdView3 w = sw;
+    float *dp = reinterpret_cast<float *>(plan + P.dp) + (size_t)v * (C + 1);
+    float *mag = reinterpret_cast<float *>(plan + P.mag) + (size_t)v * C;
+    float *rz = reinterpret_cast<float *>(plan + P.rowz) + (size_t)v * R * 2;
+    for (int k = tid; k <= C; k += kThreads) dp[k] = dd3_col_boundary(GEOM, &g, &w, k);
+    float mn = 3.0e38f, mx = -3.0e38f;
+    for (int k = tid; k < C; k += kThreads) {
+        const float m = dd3_col_mag(GEOM, &g, &w, k);
+        mag[k] = m;
+        mn = fminf(mn, m);
+        mx = fmaxf(mx, m);
+    }
+    for (int r = tid; r < R; r += kThreads) dd3_row_z(GEOM, &g, &w, r, &rz[2 * r], &rz[2 * r + 1]);
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((tid & 31) == 0) {
+        red[0][tid >> 5] = mn;
+        red[1][tid >> 5] = mx;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        DdView3 out = w;
+        out.magmin = red[0][0];
+        out.magmax = red[1][0];
+        for (int i = 1; i < kThreads / 32; i++) {
+            out.magmin = fminf(out.magmin, red[0][i]);
+            out.magmax = fmaxf(out.magmax, red[1][i]);
+        }
+        float a0, a1, b0, b1;
+        dd3_row_z(GEOM, &g, &w, 0, &a0, &a1);
+        dd3_row_z(GEOM, &g, &w, R - 1, &b0, &b1);
+        out.rzA = a0;
+        out.rzB = (R > 1) ? (b0 - a0) / (float)(R - 1) : a1 - a0;
+        reinterpret_cast<DdView3 *>(plan + P.views)[v] = out;
+    }
+}
+
+// One thread per (view, line, walk block): walk start and drift pieces.
+template <int GEOM>
+__global__ void __launch_bounds__(128) k_lines3(dd_geom3d g, char *plan, PlanLayout P) {
+    const int v = blockIdx.y;
+    const int idx = blockIdx.x * 128 + threadIdx.x;
+    const int line = idx / P.nch, cc = idx - line * P.nch;
+    const DdView3 *views = reinterpret_cast<const DdView3 *>(plan + P.views);
+    const int xb = views[v].xb;
+    const int nline = xb ? g.height : g.width;
+    if (line >= nline) return;
+    const DdView3 w = views[v];
+    const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * (g.num_col + 1);
+    DdLine *L = reinterpret_cast<DdLine *>(plan + P.lines) + ((size_t)v * P.nl + line) * P.nch + cc;
+    float lz[4];
+    dd3_line_setup(GEOM, &g, &w, dp, line, cc, lz, L);
+    if (cc == 0)
+        reinterpret_cast<float4 *>(plan + P.linez)[(size_t)v * P.nl + line] = make_float4(lz[0], lz[1], lz[2], lz[3]);
+}
+
+// volT[b][s][x][H-1-y] = vol[b][s][y][x]: walked lines of y-branch views
+// become contiguous rows.
+__global__ void __launch_bounds__(256) k_transpose3(const float *__restrict__ in, float *__restrict__ out, int W,
+                                                    int H, int nplanes) {
+    __shared__ float t[32][33];
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int pl = blockIdx.z; pl < nplanes; pl += gridDim.z) {
+        const size_t plane = (size_t)pl * W * H;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int y = y0 + ty + 8 * i, x = x0 + tx;
+            if (y < H && x < W) t[ty + 8 * i][tx] = in[plane + (size_t)y * W + x];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int x = x0 + ty + 8 * i, y = y0 + tx;
+            if (x < W && y < H) out[plane + (size_t)x * H + (H - 1 - y)] = t[tx][ty + 8 * i];
+        }
+        __syncthreads();
+    }
+}
+
+// ss[b][v][r][k] = in[b][v][r][k'] * scale(v, r, k) with k the sorted column:
+// the adjoint gathers pre-scaled bins (ConeFlatDisCUDA3d.cu:400-404).
+template <int GEOM, int FAMILY>
+__global__ void __launch_bounds__(128) k_sino3(dd_geom3d g, const char *__restrict__ plan, PlanLayout P,
+                                               const float *__restrict__ in, float *__restrict__ ss, int B, int V) {
+    const int C = g.num_col, R = g.num_row;
+    const int k = blockIdx.x * 128 + threadIdx.x, r = blockIdx.y, v = blockIdx.z;
+    if (k >= C) return;
+    const DdView3 &w = reinterpret_cast<const DdView3 *>(plan + P.views)[v];
+    float scale = w.bp_scale;
+    if (FAMILY == 0) {
+        const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * (C + 1);
+        const float *rz = reinterpret_cast<const float *>(plan + P.rowz) + (size_t)v * R * 2;
+        const float mag = reinterpret_cast<const float *>(plan + P.mag)[(size_t)v * C + k];
+        float rp0, rp1;
+        dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0, &rp1);
+        scale = dd3_proj_scale(&g, &w, dp[k], dp[k + 1], rp0, rp1);
+    }
+    const int ko = w.flip ? C - 1 - k : k;
+    const size_t per = (size_t)V * R * C;
+    const size_t row = ((size_t)v * R + r) * C;
+    for (int b = 0; b < B; b++) ss[b * per + row + k] = FMUL(in[b * per + row + ko], scale);
+}
+
+// ---------------------------------------------------------------------------
+// Forward-type kernel: detector gathers
+// ---------------------------------------------------------------------------
+struct Fwd3Args {
+    dd_geom3d g;
+    const char *plan;
+    PlanLayout P;
+    const float *vol;    // (B, Dep, H, W)
+    const float *volT;   // (B, Dep, W, H), pixel order reversed along y
+    float *out;          // (B, V, R, C)
+    const float *sub;    // optional: out = A x - sub
+    int B, V, nrb;
+};
+
+// grid: (view, walk block, row block x volume group); thread = one column of
+// the walk block (8 warps x 32 lanes = 256 columns), kRB rows, kNB volumes.
+template <int GEOM, int FAMILY>
+__global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
+    const dd_geom3d &g = a.g;
+    const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
+    const int v = blockIdx.x, cc = blockIdx.y;
+    const int rb = blockIdx.z % a.nrb, bg = blockIdx.z / a.nrb;
+    const int kk = threadIdx.x, k = cc * DD3_CHUNK + kk;
+    if (k >= C) return;
+    const int r0 = rb * kRB, b0 = bg * kNB;
+    const int nb = min(kNB, a.B - b0);
+    const PlanLayout &P = a.P;
+    const DdView3 w = reinterpret_cast<const DdView3 *>(a.plan + P.views)[v];
+    const float *__restrict__ dp = reinterpret_cast<const float *>(a.plan + P.dp) + (size_t)v * (C + 1);
+    const float *__restrict__ rz = reinterpret_cast<const float *>(a.plan + P.rowz) + (size_t)v * R * 2;
+    const float mag = reinterpret_cast<const float *>(a.plan + P.mag)[(size_t)v * C + k];
+    const float4 *__restrict__ linez = reinterpret_cast<const float4 *>(a.plan + P.linez) + (size_t)v * P.nl;
+    const DdLine *__restrict__ lines = reinterpret_cast<const DdLine *>(a.plan + P.lines) + (size_t)v * P.nl * P.nch + cc;
+
+    float rp0[kRB], rp1[kRB];
+#pragma unroll
+    for (int q = 0; q < kRB; q++) {
+        const int r = r0 + q;
+        if (r < R) {
+            dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0[q], &rp1[q]);
+        } else {
+            rp0[q] = 3.0e38f;    // empty row: the z walk never starts
+            rp1[q] = -3.0e38f;
+        }
+    }
+    float acc[kRB][kNB];
+#pragma unroll
+    for (int q = 0; q < kRB; q++)
+#pragma unroll
+        for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
+
+    const int xb = w.xb;
+    const int nline = xb ? H : W, npix = xb ? W : H;
+    const float *__restrict__ src = xb ? a.vol : a.volT;
+    const size_t plane = (size_t)nline * npix;
+    const size_t vstride = (size_t)Dp * plane;
+    src += (size_t)b0 * vstride;
+
+    for (int line = 0; line < nline; line++) {
+        const float4 lz = linez[line];
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < kRB; q++) any |= fmaxf(lz.x, rp0[q]) < fminf(lz.y, rp1[q]);
+        if (!any) continue;
+        const DdLine *L = lines + (size_t)line * P.nch;
+        DdColWalk cw;
+        if (!dd3_colwalk_init(L, dp, k, kk, &cw)) continue;
+        const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+        const float *__restrict__ lsrc = src + (size_t)line * npix;
+        bool more = true;
+        while (more) {
+            int js[kNS];
+            float cs[kNS];
+            int n = 0;
+#pragma unroll
+            for (int q = 0; q < kNS; q++) {
+                js[q] = 0;
+                cs[q] = 0.0f;
+                if (more) {
+                    int j;
+                    float wd;
+                    if (dd3_colwalk_next(L, &cw, &j, &wd)) {
+                        js[q] = j;
+                        cs[q] = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
+                        n = q + 1;
+                    } else {
+                        more = false;
+                    }
+                }
+            }
+            if (n == 0) break;
+#pragma unroll
+            for (int q = 0; q < kRB; q++) {
+                DdZ3 z;
+                dd3_zstart(lz.x, lz.y, lz.z, rp0[q], rp1[q], &z);
+                float zw;
+                int s;
+                while (dd3_zstep(&z, lz.z, Dp, &zw, &s)) {
+                    const float *__restrict__ ps = lsrc + (size_t)s * plane;
+#pragma unroll
+                    for (int t = 0; t < kNS; t++) {
+                        if (t < n) {
+                            const float wq = FMUL(zw, cs[t]);
+#pragma unroll
+                            for (int b = 0; b < kNB; b++)
+                                if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride + js[t]), acc[q][b]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const int ko = w.flip ? C - 1 - k : k;
+#pragma unroll
+    for (int q = 0; q < kRB; q++) {
+        const int r = r0 + q;
+        if (r >= R) continue;
+        const float scale = (FAMILY == 0) ? dd3_proj_scale(&g, &w, dp[k], dp[k + 1], rp0[q], rp1[q]) : w.bp_scale;
+#pragma unroll
+        for (int b = 0; b < kNB; b++) {
+            if (b < nb) {
+                const size_t o = (((size_t)(b0 + b) * a.V + v) * R + r) * C + ko;
+                float val = FMUL(acc[q][b], scale);
+                if (a.sub) val = FSUB(val, a.sub[o]);
+                a.out[o] = val;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint-type kernel: voxel gathers
+// ---------------------------------------------------------------------------
+struct Adj3Args {
+    dd_geom3d g;
+    const char *plan;
+    PlanLayout P;
+    const float *ss;     // pre-scaled sinogram (B, V, R, C), sorted columns
+    float *out;          // (B, Dep, H, W)
+    const float *base;   // optional: out = base + scale * value (may alias out)
+    float scale;
+    int B, V, ntx;
+};
+
+// grid: (voxel-column tile, slab of kZS slices, volume group); thread = one
+// (x, y) voxel column of a 16 x 16 tile.
+template <int GEOM, int FAMILY>
+__global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
+    const dd_geom3d &g = a.g;
+    const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
+    const int tX = blockIdx.x % a.ntx, tY = blockIdx.x / a.ntx;
+    const int x = tX * kTile + (threadIdx.x & (kTile - 1)), y = tY * kTile + (threadIdx.x / kTile);
+    if (x >= W || y >= H) return;
+    const int s0 = blockIdx.y * kZS, b0 = blockIdx.z * kNB;
+    const int nb = min(kNB, a.B - b0);
+    const PlanLayout &P = a.P;
+    const DdView3 *__restrict__ views = reinterpret_cast<const DdView3 *>(a.plan + P.views);
+    const float *__restrict__ dpt = reinterpret_cast<const float *>(a.plan + P.dp);
+    const float *__restrict__ magt = reinterpret_cast<const float *>(a.plan + P.mag);
+    const float *__restrict__ rzt = reinterpret_cast<const float *>(a.plan + P.rowz);
+    const float4 *__restrict__ linez = reinterpret_cast<const float4 *>(a.plan + P.linez);
+    const DdLine *__restrict__ lines = reinterpret_cast<const DdLine *>(a.plan + P.lines);
+    const size_t per = (size_t)a.V * R * C;
+    const float *__restrict__ ssb = a.ss + (size_t)b0 * per;
+    // line ranges of this CTA (for the slab visibility test)
+    const int xlo = tX * kTile, xhi = min(xlo + kTile - 1, W - 1);
+    const int ylo = tY * kTile, yhi = min(ylo + kTile - 1, H - 1);
+
+    float acc[kZS][kNB];
+#pragma unroll
+    for (int q = 0; q < kZS; q++)
+#pragma unroll
+        for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
+
+    for (int v = 0; v < a.V; v++) {
+        const DdView3 w = views[v];
+        const float *__restrict__ rz = rzt + (size_t)v * R * 2;
+        {   // can this view see the slab at all?
+            const int l0 = w.xb ? ylo : xlo, l1 = w.xb ? yhi : xhi;
+            const float m0 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l0));
+            const float m1 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l1));
+            const float zsA = w.z0 + (float)(s0 - 1) * g.pix_z, zsB = w.z0 + (float)(s0 + kZS + 1) * g.pix_z;
+            if (!dd3_slab_lit(&w, fminf(m0, m1), fmaxf(m0, m1), zsA, zsB, rz[0], rz[2 * R - 1])) continue;
+        }
+        const int line = w.xb ? y : x;
+        const int j = w.xb ? x : H - 1 - y;
+        const float4 lz = linez[(size_t)v * P.nl + line];
+        const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+        const float margin = 0.25f * fabsf(lz.z);
+        const float *__restrict__ dp = dpt + (size_t)v * (C + 1);
+        const DdLine *__restrict__ lrec = lines + ((size_t)v * P.nl + line) * P.nch;
+        const float *__restrict__ ssv = ssb + (size_t)v * R * C;
+        for (int cc = 0; cc < P.nch; cc++) {
+            DdPixWalk pw;
+            if (!dd3_pixwalk_init(GEOM, &g, &w, lrec + cc, dp, cc, j, &pw)) continue;
+            int k;
+            float wd;
+            while (dd3_pixwalk_next(dp, &pw, &k, &wd)) {
+                const float coef = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
+                const float mag = magt[(size_t)v * C + k];
+                const float *__restrict__ ssk = ssv + k;
+#pragma unroll
+                for (int q = 0; q < kZS; q++) {
+                    const int s = s0 + q;
+                    if (s < Dp) {
+                        const float zlo = FADD(lz.x, FMUL((float)s, lz.z));
+                        const float zhi = FADD(zlo, lz.z);
+                        for (int r = dd3_row_first(GEOM, &w, rz, R, mag, zlo, margin); r < R; r++) {
+                            float e0, e1;
+                            dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &e0, &e1);
+                            if (e0 >= zhi + margin) break;
+                            const float zw = dd3_zweight(lz.x, lz.y, lz.z, e0, e1, s, Dp);
+                            if (zw != 0.0f) {
+                                const float wq = FMUL(zw, coef);
+#pragma unroll
+                                for (int b = 0; b < kNB; b++)
+                                    if (b < nb) acc[q][b] = fmaf(wq, __ldg(ssk + (size_t)b * per + (size_t)r * C), acc[q][b]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kZS; q++) {
+        const int s = s0 + q;
+        if (s >= Dp) continue;
+#pragma unroll
+        for (int b = 0; b < kNB; b++) {
+            if (b < nb) {
+                const size_t o = (((size_t)(b0 + b) * Dp + s) * H + y) * W + x;
+                a.out[o] = a.base ? fmaf(a.scale, acc[q][b], a.base[o]) : acc[q][b];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+int geom_of(int scan) {
+    return scan == DD_SCAN_CONE_FLAT ? DD_GEOM3_CONE_FLAT : (scan == DD_SCAN_CONE_ARC ? DD_GEOM3_CONE_ARC : DD_GEOM3_SPIRAL);
+}
+
+int validate(int scan, int op, const dd_geom3d *g, int B, int V) {
+    if (!g) return DD_ERR_INVALID_ARG;
+    if (scan < DD_SCAN_CONE_FLAT || scan > DD_SCAN_SPIRAL) return DD_ERR_INVALID_ARG;
+    if (op < DD_OP_PROJ || op > DD_OP_BPROJ_TW) return DD_ERR_INVALID_ARG;
+    if (g->width <= 0 || g->height <= 0 || g->depth <= 0 || g->num_col <= 0 || g->num_row <= 0 || B <= 0 ||
+        V <= 0)
+        return DD_ERR_INVALID_ARG;
+    const float f[] = {g->pix_x, g->pix_y, g->pix_z, g->col_size, g->row_size, g->iso_source,
+                       g->source_detector, g->pix_xshift, g->pix_yshift, g->pix_zshift, g->col_shift,
+                       g->row_shift};
+    for (float x : f)
+        if (!(x == x) || x - x != 0.0f) return DD_ERR_INVALID_ARG;   // NaN / inf
+    if (!(g->pix_x > 0 && g->pix_y > 0 && g->pix_z > 0 && g->col_size > 0 && g->row_size > 0))
+        return DD_ERR_INVALID_ARG;
+    if (!(g->iso_source > 0 && g->source_detector > 0)) return DD_ERR_INVALID_ARG;
+    const long long lim = (1LL << 31) - 1;
+    if ((long long)g->width * g->height * g->depth * B > lim) return DD_ERR_SIZE_OVERFLOW;
+    if ((long long)V * g->num_row * g->num_col * B > lim) return DD_ERR_SIZE_OVERFLOW;
+    if (g->width > 8192 || g->height > 8192 || V > 65535 || g->num_row > 65535 || g->num_col > 65535)
+        return DD_ERR_SIZE_OVERFLOW;
+    return DD_OK;
+}
+
+int launch_status() {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? DD_OK : DD_ERR_LAUNCH;
+}
+
+int plan(int scan, const dd_geom3d *g, const float *angles, const float *sp, int V, void *planp, size_t bytes,
+         cudaStream_t st) {
+    const PlanLayout P = plan_layout(g, V);
+    if (!planp || bytes < P.total) return DD_ERR_WORKSPACE;
+    if (!angles || (scan == DD_SCAN_SPIRAL && !sp)) return DD_ERR_INVALID_ARG;
+    char *base = (char *)planp;
+    const int geom = geom_of(scan);
+    dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_PLAN, st);
+    const dim3 gl((unsigned)((P.nl * P.nch + 127) / 128), (unsigned)V);
+    if (geom == DD_GEOM3_CONE_FLAT) {
+        k_views3<DD_GEOM3_CONE_FLAT><<<V, kThreads, 0, st>>>(*g, angles, sp, V, base, P);
+        k_lines3<DD_GEOM3_CONE_FLAT><<<gl, 128, 0, st>>>(*g, base, P);
+    } else if (geom == DD_GEOM3_CONE_ARC) {
+        k_views3<DD_GEOM3_CONE_ARC><<<V, kThreads, 0, st>>>(*g, angles, sp, V, base, P);
+        k_lines3<DD_GEOM3_CONE_ARC><<<gl, 128, 0, st>>>(*g, base, P);
+    } else {
+        k_views3<DD_GEOM3_SPIRAL><<<V, kThreads, 0, st>>>(*g, angles, sp, V, base, P);
+        k_lines3<DD_GEOM3_SPIRAL><<<gl, 128, 0, st>>>(*g, base, P);
+    }
+    dd2::prof_end(pr, st);
+    dd2::count_launches(2);
+    return launch_status();
+}
+
+template <int GEOM>
+int launch_fwd(int family, const Fwd3Args &a, cudaStream_t st) {
+    const dim3 grid((unsigned)a.V, (unsigned)a.P.nch, (unsigned)(a.nrb * ((a.B + kNB - 1) / kNB)));
+    dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_FORWARD, st);
+    if (family == 0) k_fwd3<GEOM, 0><<<grid, kThreads, 0, st>>>(a);
+    else if (family == 1) k_fwd3<GEOM, 1><<<grid, kThreads, 0, st>>>(a);
+    else k_fwd3<GEOM, 2><<<grid, kThreads, 0, st>>>(a);
+    dd2::prof_end(pr, st);
+    dd2::count_launches(1);
+    return launch_status();
+}
+
+template <int GEOM>
+int launch_adj(int family, const Adj3Args &a, const float *in, float *ss, cudaStream_t st) {
+    const dd_geom3d &g = a.g;
+    const dim3 gs((unsigned)((g.num_col + 127) / 128), (unsigned)g.num_row, (unsigned)a.V);
+    dd2::ProfRec *pt = dd2::prof_begin(DD_KERNEL_TABLES, st);
+    if (family == 0) k_sino3<GEOM, 0><<<gs, 128, 0, st>>>(g, a.plan, a.P, in, ss, a.B, a.V);
+    else k_sino3<GEOM, 1><<<gs, 128, 0, st>>>(g, a.plan, a.P, in, ss, a.B, a.V);
+    dd2::prof_end(pt, st);
+    const int nty = (g.height + kTile - 1) / kTile;
+    const dim3 grid((unsigned)(a.ntx * nty), (unsigned)((g.depth + kZS - 1) / kZS), (unsigned)((a.B + kNB - 1) / kNB));
+    dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_ADJOINT, st);
+    if (family == 0) k_adj3<GEOM, 0><<<grid, kThreads, 0, st>>>(a);
+    else if (family == 1) k_adj3<GEOM, 1><<<grid, kThreads, 0, st>>>(a);
+    else k_adj3<GEOM, 2><<<grid, kThreads, 0, st>>>(a);
+    dd2::prof_end(pr, st);
+    dd2::count_launches(2);
+    return launch_status();
+}
+
+int transpose(const dd_geom3d *g, const float *in, float *out, int B, cudaStream_t st) {
+    const int np = B * g->depth;
+    const dim3 grid((unsigned)((g->width + 31) / 32), (unsigned)((g->height + 31) / 32),
+                    (unsigned)(np < 65535 ? np : 65535));
+    dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_TABLES, st);
+    k_transpose3<<<grid, 256, 0, st>>>(in, out, g->width, g->height, np);
+    dd2::prof_end(pr, st);
+    dd2::count_launches(1);
+    return launch_status();
+}
+
+// Forward-type operator into `out` (optionally minus `sub`).
+int forward(int scan, int op, const dd_geom3d *g, const char *planb, const float *in, float *out,
+            const float *sub, int B, int V, char *volT, cudaStream_t st) {
+    const int s1 = transpose(g, in, (float *)volT, B, st);
+    if (s1 != DD_OK) return s1;
+    Fwd3Args a;
+    a.g = *g;
+    a.plan = planb;
+    a.P = plan_layout(g, V);
+    a.vol = in;
+    a.volT = (const float *)volT;
+    a.out = out;
+    a.sub = sub;
+    a.B = B;
+    a.V = V;
+    a.nrb = (g->num_row + kRB - 1) / kRB;
+    const int fam = op_family(op), geom = geom_of(scan);
+    if (geom == DD_GEOM3_CONE_FLAT) return launch_fwd<DD_GEOM3_CONE_FLAT>(fam, a, st);
+    if (geom == DD_GEOM3_CONE_ARC) return launch_fwd<DD_GEOM3_CONE_ARC>(fam, a, st);
+    return launch_fwd<DD_GEOM3_SPIRAL>(fam, a, st);
+}
+
+// Adjoint-type operator: out = value, or out = base + scale * value.
+int adjoint(int scan, int op, const dd_geom3d *g, const char *planb, const float *in, float *out,
+            const float *basep, float scale, int B, int V, char *ss, cudaStream_t st) {
+    Adj3Args a;
+    a.g = *g;
+    a.plan = planb;
+    a.P = plan_layout(g, V);
+    a.ss = (const float *)ss;
+    a.out = out;
+    a.base = basep;
+    a.scale = scale;
+    a.B = B;
+    a.V = V;
+    a.ntx = (g->width + kTile - 1) / kTile;
+    const int fam = op_family(op), geom = geom_of(scan);
+    if (geom == DD_GEOM3_CONE_FLAT) return launch_adj<DD_GEOM3_CONE_FLAT>(fam, a, in, (float *)ss, st);
+    if (geom == DD_GEOM3_CONE_ARC) return launch_adj<DD_GEOM3_CONE_ARC>(fam, a, in, (float *)ss, st);
+    return launch_adj<DD_GEOM3_SPIRAL>(fam, a, in, (float *)ss, st);
+}
+
+}   // namespace dd3
+
+using namespace dd3;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int dd3d_validate(int scan, int op, const dd_geom3d *g, int batch, int num_view) {
+    return validate(scan, op, g, batch, num_view);
+}
+
+extern "C" size_t dd3d_plan_bytes(int scan, const dd_geom3d *g, int num_view) {
+    (void)scan;
+    if (!g || num_view <= 0) return 0;
+    return plan_layout(g, num_view).total;
+}
+
+extern "C" int dd3d_plan(int scan, const dd_geom3d *g, const float *angles, const float *source_pos, int num_view,
+                         void *planp, size_t plan_bytes, dd_stream_t stream) {
+    const int st = validate(scan, DD_OP_PROJ, g, 1, num_view);
+    if (st != DD_OK) return st;
+    return plan(scan, g, angles, source_pos, num_view, planp, plan_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t dd3d_apply_workspace_bytes(int scan, int op, const dd_geom3d *g, int batch, int num_view) {
+    (void)scan;
+    if (!g || batch <= 0 || num_view <= 0) return 0;
+    const bool f = op_is_forward(op);
+    return apply_layout(f, !f, g, batch, num_view).total;
+}
+
+extern "C" int dd3d_apply_planned(int scan, int op, const dd_geom3d *g, const void *planp, const float *in,
+                                  float *out, int batch, int num_view, void *workspace, size_t workspace_bytes,
+                                  dd_stream_t stream) {
+    const int st = validate(scan, op, g, batch, num_view);
+    if (st != DD_OK) return st;
+    if (!planp || !in || !out) return DD_ERR_INVALID_ARG;
+    const bool f = op_is_forward(op);
+    const ApplyLayout A = apply_layout(f, !f, g, batch, num_view);
+    if (!workspace || workspace_bytes < A.total) return DD_ERR_WORKSPACE;
+    char *wb = (char *)workspace;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (f) return forward(scan, op, g, (const char *)planp, in, out, nullptr, batch, num_view, wb + A.volT, s);
+    return adjoint(scan, op, g, (const char *)planp, in, out, nullptr, 0.0f, batch, num_view, wb + A.ss, s);
+}
+
+extern "C" size_t dd3d_workspace_bytes(int scan, int op, const dd_geom3d *g, int batch, int num_view) {
+    if (!g || batch <= 0 || num_view <= 0) return 0;
+    return dd3d_plan_bytes(scan, g, num_view) + dd3d_apply_workspace_bytes(scan, op, g, batch, num_view);
+}
+
+extern "C" int dd3d_apply(int scan, int op, const dd_geom3d *g, const float *in, float *out, const float *angles,
+                          const float *source_pos, int batch, int num_view, void *workspace,
+                          size_t workspace_bytes, dd_stream_t stream) {
+    const int st = validate(scan, op, g, batch, num_view);
+    if (st != DD_OK) return st;
+    if (!in || !out || !angles || (scan == DD_SCAN_SPIRAL && !source_pos)) return DD_ERR_INVALID_ARG;
+    const size_t pb = dd3d_plan_bytes(scan, g, num_view);
+    if (!workspace || workspace_bytes < dd3d_workspace_bytes(scan, op, g, batch, num_view)) return DD_ERR_WORKSPACE;
+    const int s1 = plan(scan, g, angles, source_pos, num_view, workspace, pb, (cudaStream_t)stream);
+    if (s1 != DD_OK) return s1;
+    return dd3d_apply_planned(scan, op, g, workspace, in, out, batch, num_view, (char *)workspace + pb,
+                              workspace_bytes - pb, stream);
+}
+
+extern "C" size_t dd3d_dc_workspace_bytes(int scan, const dd_geom3d *g, int batch, int num_view) {
+    (void)scan;
+    if (!g || batch <= 0 || num_view <= 0) return 0;
+    return apply_layout(true, true, g, batch, num_view).total;
+}
+
+extern "C" int dd3d_dc_step(int scan, const dd_geom3d *g, const void *planp, float *x, const float *y, float *resid,
+                            float eta, int batch, int num_view, void *workspace, size_t workspace_bytes,
+                            dd_stream_t stream) {
+    const int st = validate(scan, DD_OP_PROJ, g, batch, num_view);
+    if (st != DD_OK) return st;
+    if (!planp || !x || !y || !resid) return DD_ERR_INVALID_ARG;
+    const ApplyLayout A = apply_layout(true, true, g, batch, num_view);
+    if (!workspace || workspace_bytes < A.total) return DD_ERR_WORKSPACE;
+    char *wb = (char *)workspace;
+    cudaStream_t s = (cudaStream_t)stream;
+    const char *pb = (const char *)planp;
+    const int s1 = forward(scan, DD_OP_PROJ, g, pb, x, resid, y, batch, num_view, wb + A.volT, s);
+    if (s1 != DD_OK) return s1;
+    return adjoint(scan, DD_OP_PROJ_T, g, pb, resid, x, x, -eta, batch, num_view, wb + A.ss, s);
+}
+
+// named entries (RadonTorch.cpp:1395-1414)
+#define DD_NAMED3(name, scan, op)                                                                          \
+    extern "C" int dd_##name(const dd_geom3d *g, const float *in, float *out, const float *angles,           \
+                             const float *source_pos, int batch, int num_view, void *workspace,             \
+                             size_t workspace_bytes, dd_stream_t stream) {                                  \
+        return dd3d_apply(scan, op, g, in, out, angles, source_pos, batch, num_view, workspace,            \
+                          workspace_bytes, stream);                                                         \
+    }
+DD_NAMED3(ProjConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_PROJ)
+DD_NAMED3(ProjTransConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_PROJ_T)
+DD_NAMED3(BackProjConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_BPROJ)
+DD_NAMED3(BackProjTransConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_BPROJ_T)
+DD_NAMED3(BackProjWeightedConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_BPROJ_W)
+DD_NAMED3(BackProjTransWeightedConeFlatDis3d, DD_SCAN_CONE_FLAT, DD_OP_BPROJ_TW)
+DD_NAMED3(ProjConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_PROJ)
+DD_NAMED3(ProjTransConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_PROJ_T)
+DD_NAMED3(BackProjConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_BPROJ)
+DD_NAMED3(BackProjTransConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_BPROJ_T)
+DD_NAMED3(BackProjWeightedConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_BPROJ_W)
+DD_NAMED3(BackProjTransWeightedConeArcDis3d, DD_SCAN_CONE_ARC, DD_OP_BPROJ_TW)
+DD_NAMED3(ProjSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_PROJ)
+DD_NAMED3(ProjTransSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_PROJ_T)
+DD_NAMED3(BackProjSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_BPROJ)
+DD_NAMED3(BackProjTransSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_BPROJ_T)
+DD_NAMED3(BackProjWeightedSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_BPROJ_W)
+DD_NAMED3(BackProjTransWeightedSpiralDis3d, DD_SCAN_SPIRAL, DD_OP_BPROJ_TW)
+#undef DD_NAMED3

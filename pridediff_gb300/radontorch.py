@@ -153,6 +153,63 @@ def _apply2d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor)
     return out
 
 
+def plan3d(scan: str, g, angles: torch.Tensor, source_pos=None):
+    """Device plan of a 3-D geometry (cached; spiral plans also key on the
+    source table's identity and version)."""
+    lib = N.load()
+    sc = N.SCAN3D[scan]
+    V = int(angles.shape[0])
+    sp_key = None if source_pos is None else (id(source_pos), source_pos._version)
+    key = ("3d", sc, tuple(getattr(g, f) for f, _ in g._fields_), V, angles.device.index, sp_key)
+
+    def build():
+        nbytes = int(lib.dd3d_plan_bytes(sc, g, V))
+        plan = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=angles.device)
+        N.check(lib.dd3d_plan(sc, g, angles.data_ptr(), source_pos.data_ptr() if source_pos is not None else None,
+                              V, plan.data_ptr(), nbytes, _stream_ptr(angles.device)), f"{scan} plan")
+        # keep the source table alive as long as the plan is cached
+        return (plan, source_pos) if source_pos is not None else plan
+
+    entry = plans.get(key, angles, build)
+    return entry[0] if isinstance(entry, tuple) else entry
+
+
+def _apply3d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor, source_pos=None) -> torch.Tensor:
+    _check_inputs(x, angles, source_pos)
+    if source_pos is not None and source_pos.dtype != torch.float32:
+        raise RuntimeError("Expected float32 tensors")
+    lib = N.load()
+    o = host_options(options)
+    g = N.geom3d(o, spiral=(scan == "spiral"))
+    if x.dim() != 5:
+        raise RuntimeError("expected a 5-D (B, C, ., ., .) tensor")
+    B, Ch = x.shape[0], x.shape[1]
+    V = angles.shape[0]
+    if scan == "spiral" and (source_pos is None or tuple(source_pos.shape) != (4, V)):
+        raise RuntimeError("source_pos must be a (4, V) tensor")
+    image_in = op in ("proj", "bproj_t", "bproj_tw")
+    if image_in:
+        if tuple(x.shape[2:]) != (g.depth, g.height, g.width):
+            raise RuntimeError("image size inconsistent with options")
+        out = torch.empty((B, Ch, V, g.num_row, g.num_col), dtype=torch.float32, device=x.device)
+    else:
+        if tuple(x.shape[2:]) != (V, g.num_row, g.num_col):
+            raise RuntimeError("sinogram size inconsistent with options and angles")
+        out = torch.empty((B, Ch, g.depth, g.height, g.width), dtype=torch.float32, device=x.device)
+    if B * Ch == 0:
+        return out.zero_()
+    sc, opc = N.SCAN3D[scan], N.OPS[op]
+    with torch.cuda.device(x.device):
+        N.check(lib.dd3d_validate(sc, opc, g, B * Ch, V), f"{scan} {op}")
+        plan = plan3d(scan, g, angles, source_pos)
+        nbytes = int(lib.dd3d_apply_workspace_bytes(sc, opc, g, B * Ch, V))
+        ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+        st = lib.dd3d_apply_planned(sc, opc, g, plan.data_ptr(), x.data_ptr(), out.data_ptr(), B * Ch, V,
+                                    ws.data_ptr(), nbytes, _stream_ptr(x.device))
+    N.check(st, f"{scan} {op}")
+    return out
+
+
 def _not_yet(name):
     def f(*args, **kwargs):
         raise NotImplementedError(f"radontorch.{name} is not available in this build")
@@ -186,13 +243,28 @@ for _pre, _op in (("Proj", "proj"), ("ProjTrans", "proj_t"), ("BackProj", "bproj
     globals()[_name] = _mk2("para", _op, _name)
 
 # ---------------------------------------------------------------------------
-# 3-D operators (RadonTorch.cpp:1395-1414) -- provided by the 3-D library
+# 3-D operators (RadonTorch.cpp:1395-1414)
 # ---------------------------------------------------------------------------
-NAMES3D = [f"{pre}{geo}Dis3d" for geo in ("ConeFlat", "ConeArc", "Spiral")
-           for pre in ("Proj", "ProjTrans", "BackProj", "BackProjTrans", "BackProjWeighted",
-                       "BackProjTransWeighted")]
-for _name in NAMES3D:
-    globals()[_name] = _not_yet(_name)
+def _mk3(scan, op, name):
+    if scan == "spiral":
+        def f(input, options, angles, source_pos):
+            return _apply3d(scan, op, input, options, angles, source_pos)
+    else:
+        def f(input, options, angles):
+            return _apply3d(scan, op, input, options, angles)
+    f.__name__ = name
+    f.__doc__ = f"Replaces radontorch.{name} (deeprecon/interface/RadonTorch.cpp)."
+    return f
+
+
+NAMES3D = []
+for _geo, _s in (("ConeFlat", "cone_flat"), ("ConeArc", "cone_arc"), ("Spiral", "spiral")):
+    for _pre, _op in (("Proj", "proj"), ("ProjTrans", "proj_t"), ("BackProj", "bproj"),
+                      ("BackProjTrans", "bproj_t"), ("BackProjWeighted", "bproj_w"),
+                      ("BackProjTransWeighted", "bproj_tw")):
+        _name = f"{_pre}{_geo}Dis3d"
+        globals()[_name] = _mk3(_s, _op, _name)
+        NAMES3D.append(_name)
 
 # ---------------------------------------------------------------------------
 # System matrices (RadonTorch.cpp:1270-1372)

@@ -104,3 +104,54 @@ def host_model():
         if r.returncode != 0:
             pytest.skip("host model does not compile here: " + r.stderr[-400:])
     return HostModel(so)
+
+
+class _G3(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("width", "height", "depth", "num_col", "num_row")] + \
+        [(n, ctypes.c_float) for n in ("pix_x", "pix_y", "pix_z", "col_size", "row_size", "iso_source",
+                                        "source_detector", "pix_xshift", "pix_yshift", "pix_zshift",
+                                        "col_shift", "row_shift")]
+
+
+class HostModel3:
+    """ctypes wrapper of tests/native/dd_model3d.cpp (host model of the 3-D kernels)."""
+    OPS = {"proj": 0, "proj_t": 1, "bproj": 2, "bproj_t": 3, "bproj_w": 4, "bproj_tw": 5}
+    SCAN = {"cone_flat": 0, "cone_arc": 1, "spiral": 2}
+
+    def __init__(self, path):
+        self.lib = ctypes.CDLL(path)
+        fp = ctypes.POINTER(ctypes.c_float)
+        self.lib.model_apply3d.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_G3), fp, fp, fp, fp,
+                                           ctypes.c_int, ctypes.c_int]
+
+    def apply3d(self, geom, op, x, angles, opt, source_pos=None):
+        fp = ctypes.POINTER(ctypes.c_float)
+        o = [float(v) for v in opt]
+        if geom == "spiral":
+            o = o[:14] + [0.0] + o[14:]
+        g = _G3(*[int(v) for v in o[:5]], *o[5:])
+        V, B = len(angles), x.shape[0]
+        shape = (B, V, g.num_row, g.num_col) if op in ("proj", "bproj_t", "bproj_tw") else \
+            (B, g.depth, g.height, g.width)
+        out = np.zeros(shape, np.float32)
+        x = np.ascontiguousarray(x, np.float32)
+        a = np.ascontiguousarray(angles, np.float32)
+        sp = None if source_pos is None else np.ascontiguousarray(source_pos, np.float32).ctypes.data_as(fp)
+        rc = self.lib.model_apply3d(self.SCAN[geom], self.OPS[op], ctypes.byref(g), a.ctypes.data_as(fp), sp,
+                                    x.ctypes.data_as(fp), out.ctypes.data_as(fp), B, V)
+        assert rc == 0
+        return out
+
+
+@pytest.fixture(scope="session")
+def host_model3():
+    src = os.path.join(ROOT, "tests", "native", "dd_model3d.cpp")
+    outdir = os.path.join(ROOT, "tests", "native", "_build")
+    os.makedirs(outdir, exist_ok=True)
+    so = os.path.join(outdir, "libddmodel3d.so")
+    deps = [src] + [os.path.join(ROOT, "pridediff_gb300", "csrc", f)
+                    for f in ("dd_geom.cuh", "dd_geom3d.cuh")]
+    if not os.path.exists(so) or os.path.getmtime(so) < max(os.path.getmtime(d) for d in deps):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", so],
+                       check=True)
+    return HostModel3(so)

@@ -91,3 +91,43 @@ def test_workspace_sizes_scale_with_problem(lib):
     b = lib.dd2d_apply_workspace_bytes(1, 0, g, 8, 90)
     assert b > a > 0
     assert lib.dd2d_plan_bytes(1, g, 180) > lib.dd2d_plan_bytes(1, g, 90)
+
+
+def _g3(**kw):
+    from pridediff_gb300 import _native
+    base = dict(width=64, height=64, depth=32, num_col=128, num_row=64, pix_x=1.0, pix_y=1.0, pix_z=1.0,
+                col_size=1.0, row_size=1.0, iso_source=500.0, source_detector=1000.0, pix_xshift=0.0,
+                pix_yshift=0.0, pix_zshift=0.0, col_shift=0.0, row_shift=0.0)
+    base.update(kw)
+    return _native.Geom3d(**base)
+
+
+def test_validation_3d_without_device(lib):
+    from pridediff_gb300 import _native as N
+    ok = _g3()
+    for scan in range(3):
+        for op in range(6):
+            assert lib.dd3d_validate(scan, op, ok, 2, 90) == N.DD_OK
+    assert lib.dd3d_validate(0, 0, None, 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(3, 0, ok, 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 6, ok, 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, _g3(depth=0), 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, _g3(pix_z=-1.0), 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, _g3(row_size=math.nan), 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, _g3(col_shift=math.inf), 2, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, ok, 0, 90) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_validate(0, 0, _g3(width=2048, height=2048, depth=1024), 1, 90) == N.DD_ERR_SIZE_OVERFLOW
+    assert lib.dd3d_validate(0, 0, ok, 1, 70000) == N.DD_ERR_SIZE_OVERFLOW
+
+
+def test_apply_3d_rejects_missing_workspace_and_pointers(lib):
+    from pridediff_gb300 import _native as N
+    g = _g3()
+    fake = ctypes.c_void_p(0x1000)
+    # spiral needs its source table; every entry needs a workspace
+    assert lib.dd3d_apply(2, 0, g, fake, fake, fake, None, 1, 10, fake, 1 << 40, None) == N.DD_ERR_INVALID_ARG
+    assert lib.dd3d_apply(0, 0, g, fake, fake, fake, None, 1, 10, None, 0, None) == N.DD_ERR_WORKSPACE
+    assert lib.dd3d_apply(0, 0, g, None, fake, fake, None, 1, 10, fake, 1 << 40, None) == N.DD_ERR_INVALID_ARG
+    need = lib.dd3d_workspace_bytes(0, 0, g, 1, 10)
+    assert need > lib.dd3d_plan_bytes(0, g, 10) > 0
+    assert lib.dd3d_apply(0, 0, g, fake, fake, fake, None, 1, 10, fake, need - 1, None) == N.DD_ERR_WORKSPACE

@@ -1,0 +1,208 @@
+"""GPU parity of the 3-D operators (cone-flat, cone-arc, spiral) through the
+radontorch drop-in and the C ABI.
+
+The reference has no CPU path for 3-D (RadonTorch.cpp:604); the oracle is
+the C restatement of its CUDA kernels (parity against those kernels is
+unpinned).  Bars: rel-L2 <= 1e-5 against the FP32 oracle (the error against
+the FP64 oracle is printed), dot-product adjointness <= 1e-6 with FP64
+accumulation, bit-identical repeated runs.
+"""
+import numpy as np
+import pytest
+import torch
+
+import cases3d
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+CASES = cases3d.cases()
+GEO = {"cone_flat": "ConeFlat", "cone_arc": "ConeArc", "spiral": "Spiral"}
+NAMES = {"proj": "Proj{}Dis3d", "proj_t": "ProjTrans{}Dis3d", "bproj": "BackProj{}Dis3d",
+         "bproj_t": "BackProjTrans{}Dis3d", "bproj_w": "BackProjWeighted{}Dis3d",
+         "bproj_tw": "BackProjTransWeighted{}Dis3d"}
+
+
+def run(geom, op, x, angles, opt, sp=None):
+    from pridediff_gb300 import radontorch
+    fn = getattr(radontorch, NAMES[op].format(GEO[geom]))
+    xt = torch.from_numpy(np.ascontiguousarray(x)[:, None]).cuda()
+    at = torch.from_numpy(np.ascontiguousarray(angles, np.float32)).cuda()
+    ot = torch.tensor(np.asarray(opt, np.float32))
+    if geom == "spiral":
+        out = fn(xt, ot, at, torch.from_numpy(np.ascontiguousarray(sp, np.float32)).cuda())
+    else:
+        out = fn(xt, ot, at)
+    torch.cuda.synchronize()
+    return out[:, 0].cpu().numpy()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("op", cases3d.OPS)
+def test_gpu_matches_oracle(oracle_mod, name, op):
+    geom, opt, ang, sp = CASES[name]
+    x, y = cases3d.inputs(CASES[name], batch=3, seed=11)
+    inp = x if op in cases3d.IMAGE_IN else y
+    out = run(geom, op, inp, ang, opt, sp)
+    ref = oracle_mod.run3d(geom, op, inp, ang, opt, source_pos=sp, prec="f", nthreads=8)
+    r64 = oracle_mod.run3d(geom, op, inp, ang, opt, source_pos=sp, prec="d", nthreads=8)
+    e32, e64 = rel_l2(out, ref), rel_l2(out, r64)
+    print(f"{name} {op}: rel-L2 vs FP32 oracle {e32:.2e}, vs FP64 {e64:.2e}")
+    assert e32 <= 1e-5
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_pairs_are_adjoint(name):
+    geom, opt, ang, sp = CASES[name]
+    x, y = cases3d.inputs(CASES[name], batch=2, seed=13)
+    for fwd, adj in (("proj", "proj_t"), ("bproj_t", "bproj"), ("bproj_tw", "bproj_w")):
+        ax = run(geom, fwd, x, ang, opt, sp).astype(np.float64)
+        aty = run(geom, adj, y, ang, opt, sp).astype(np.float64)
+        lhs, rhs = float((ax * y).sum()), float((x * aty).sum())
+        print(f"{name} {fwd}/{adj}: dot rel {abs(lhs - rhs) / abs(lhs):.2e}")
+        assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
+
+
+def test_gpu_runs_are_deterministic():
+    geom, opt, ang, sp = CASES["spiral_blocks"]
+    x, y = cases3d.inputs(CASES["spiral_blocks"], batch=2, seed=17)
+    for op, inp in (("proj", x), ("proj_t", y)):
+        a = run(geom, op, inp, ang, opt, sp)
+        b = run(geom, op, inp, ang, opt, sp)
+        assert np.array_equal(a, b)
+
+
+def _ellipsoids(D, H, W, n, rng):
+    zz, yy, xx = np.mgrid[0:D, 0:H, 0:W].astype(np.float64)
+    vol = np.zeros((D, H, W))
+    for _ in range(n):
+        c = [rng.uniform(0.2, 0.8) * s for s in (D, H, W)]
+        ax = [rng.uniform(0.05, 0.3) * s for s in (D, H, W)]
+        vol[((zz - c[0]) / ax[0]) ** 2 + ((yy - c[1]) / ax[1]) ** 2 + ((xx - c[2]) / ax[2]) ** 2 <= 1] += rng.uniform(0, 1)
+    return vol.astype(np.float32)
+
+
+def test_cone_flat_full_geometry_subset_of_views(oracle_mod):
+    """256^3 volume, 512 x 384 detector, SID 500 / SDD 1000 (the cone-beam
+    configuration), on 4 of its 360 views: GPU against the FP32 oracle."""
+    opt = np.array([256, 256, 256, 512, 384, 1.0, 1.0, 1.0, 1.0, 1.0, 500.0, 1000.0, 0, 0, 0, 0, 0], np.float32)
+    ang = (np.arange(360) * 2 * np.pi / 360).astype(np.float32)[[0, 45, 100, 271]]
+    x = _ellipsoids(256, 256, 256, 12, np.random.default_rng(4))[None]
+    out = run("cone_flat", "proj", x, ang, opt)
+    ref = oracle_mod.run3d("cone_flat", "proj", x, ang, opt, prec="f", nthreads=4)
+    e = rel_l2(out, ref)
+    print(f"cone-flat 256^3 proj, 4 views: rel-L2 vs FP32 oracle {e:.2e}")
+    assert e <= 1e-5
+    y = np.random.default_rng(5).random(out.shape).astype(np.float32)
+    bt = run("cone_flat", "proj_t", y, ang, opt)
+    ref = oracle_mod.run3d("cone_flat", "proj_t", y, ang, opt, prec="f", nthreads=1)
+    e = rel_l2(bt, ref)
+    print(f"cone-flat 256^3 proj_t, 4 views: rel-L2 vs FP32 oracle {e:.2e}")
+    assert e <= 1e-5
+
+
+def test_spiral_full_geometry_subset_of_views(oracle_mod):
+    """512 x 512 x 128 volume at 0.66 x 0.66 x 1.0 mm, 64 x 736 arc detector,
+    1152 views per turn, pitch 1 (the spiral configuration), on 6 of its
+    3456 views: GPU against the FP32 oracle."""
+    V = 3456
+    p = 1.0 * 64 * 1.0 * 595.0 / 1085.6 / 1152
+    z0 = -p * (V - 1) / 2
+    opt = np.array([512, 512, 128, 736, 64, 0.66, 0.66, 1.0, 1.2858 / 1085.6, 1.0, 595.0, 1085.6, 0.0, 0.0, 0.0, 0.0],
+                   np.float32)
+    sel = np.array([0, 700, 1500, 1728, 2600, 3455])
+    ang = (np.arange(V) * 2 * np.pi / 1152).astype(np.float32)[sel]
+    sp = cases3d.spiral_source(V, p, z0)[:, sel].copy()
+    x = (_ellipsoids(128, 512, 512, 12, np.random.default_rng(6)) * 0.04)[None]
+    out = run("spiral", "proj", x, ang, opt, sp)
+    ref = oracle_mod.run3d("spiral", "proj", x, ang, opt, source_pos=sp, prec="f", nthreads=6)
+    e = rel_l2(out, ref)
+    print(f"spiral 512x512x128 proj, 6 views: rel-L2 vs FP32 oracle {e:.2e}")
+    assert e <= 1e-5
+
+
+def test_projector3d_autograd_gradient_is_the_adjoint():
+    import pridediff_gb300 as P
+    proj = P.projector3d((32, 28, 20), (48, 24), 1.0, 1.0, 300.0, 600.0, scan_type="flat").cuda()
+    ang = torch.arange(16, dtype=torch.float32, device="cuda") * (2 * np.pi / 16)
+    x = torch.rand((2, 1, 20, 28, 32), device="cuda", requires_grad=True)
+    y = proj.projection(x, ang)
+    w = torch.randn_like(y)
+    (y * w).sum().backward()
+    assert torch.equal(x.grad, proj.projection_t(w, ang))
+    # central finite differences of the quadratic loss ||Ax - b||^2 at a few voxels
+    b = torch.rand_like(y)
+    x0 = x.detach().clone()
+    xr = x0.clone().requires_grad_(True)
+    ((proj.projection(xr, ang) - b) ** 2).sum().backward()
+    rng = np.random.default_rng(3)
+    h = 0.05
+    for _ in range(8):
+        idx = tuple(int(rng.integers(0, s)) for s in x0.shape)
+        xp, xm = x0.clone(), x0.clone()
+        xp[idx] += h
+        xm[idx] -= h
+        with torch.no_grad():
+            lp = ((proj.projection(xp, ang) - b).double() ** 2).sum()
+            lm = ((proj.projection(xm, ang) - b).double() ** 2).sum()
+        fd = float((lp - lm) / (2 * h))
+        g = float(xr.grad[idx])
+        assert abs(fd - g) <= 1e-3 * max(1.0, abs(g))
+
+
+def test_projectorsp_autograd_and_arc_flip():
+    import pridediff_gb300 as P
+    proj = P.projectorsp((24, 24, 16), (40, 8), (1.2, 1.2, 1.0), (1.6, 1.0), 300.0, 600.0).cuda()
+    V = 20
+    ang = torch.arange(V, dtype=torch.float32, device="cuda") * (2 * np.pi / 10)
+    sp = torch.from_numpy(cases3d.spiral_source(V, 0.8, -8.0)).cuda()
+    x = torch.rand((1, 2, 16, 24, 24), device="cuda", requires_grad=True)
+    y = proj.projection(x, ang, sp)
+    w = torch.randn_like(y)
+    (y * w).sum().backward()
+    assert torch.equal(x.grad, proj.projection_t(w, ang, sp))
+
+
+def test_dc_step_3d_matches_separate_operators():
+    import ctypes
+    from pridediff_gb300 import _native as N
+    from pridediff_gb300 import radontorch as RT
+    geom, opt, ang, sp = CASES["spiral_blocks"]
+    lib = N.load()
+    g = N.geom3d([float(v) for v in opt], spiral=True)
+    V = len(ang)
+    B = 2
+    x, y = cases3d.inputs(CASES["spiral_blocks"], batch=B, seed=23)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.from_numpy(y).cuda() * 10.0
+    at = torch.from_numpy(ang).cuda()
+    spt = torch.from_numpy(sp).cuda()
+    plan = RT.plan3d("spiral", g, at, spt)
+    nbytes = int(lib.dd3d_dc_workspace_bytes(2, g, B, V))
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    resid = torch.empty_like(yt)
+    eta = 1e-3
+    xs = xt.clone()
+    st = lib.dd3d_dc_step(2, g, plan.data_ptr(), xs.data_ptr(), yt.data_ptr(), resid.data_ptr(),
+                          ctypes.c_float(eta), B, V, ws.data_ptr(), nbytes, torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    ot = torch.tensor(opt)
+    ax = RT.ProjSpiralDis3d(xt[:, None], ot, at, spt)[:, 0]
+    assert torch.equal(resid, ax - yt)
+    expect = xt - eta * RT.ProjTransSpiralDis3d((ax - yt)[:, None], ot, at, spt)[:, 0]
+    assert rel_l2(xs.cpu().numpy(), expect.cpu().numpy()) <= 1e-6
+
+
+def test_3d_errors():
+    from pridediff_gb300 import radontorch as RT
+    opt = torch.tensor([8, 8, 4, 16, 4, 1, 1, 1, 1, 1, 100, 200, 0, 0, 0, 0, 0], dtype=torch.float32)
+    ang = torch.zeros(4, device="cuda")
+    with pytest.raises(RuntimeError):
+        RT.ProjConeFlatDis3d(torch.zeros((1, 1, 4, 8, 8)), opt, ang)            # CPU tensor
+    with pytest.raises(RuntimeError):
+        RT.ProjConeFlatDis3d(torch.zeros((1, 1, 4, 8, 9), device="cuda"), opt, ang)   # size mismatch
+    bad = opt.clone()
+    bad[5] = -1.0
+    with pytest.raises(RuntimeError):
+        RT.ProjConeFlatDis3d(torch.zeros((1, 1, 4, 8, 8), device="cuda"), bad, ang)   # negative pixel
