@@ -160,7 +160,7 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
 }
 
 // Single-geometry forward launch: grid (views, image groups).
-template <int GEOM, int WEIGHTED>
+template <int GEOM, int WEIGHTED, int NPASS>
 __global__ void __launch_bounds__(kThreads)
 k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ views,
       const float *__restrict__ dp, const float *__restrict__ bcoef,
@@ -188,7 +188,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED>(g, op, it, smem, g.num_det, rsmax, uses) && threadIdx.x == 0)
+    if (!fwd_view<GEOM, WEIGHTED, NPASS>(g, op, it, smem, g.num_det, rsmax, uses) && threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
@@ -320,7 +320,15 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const float *bc = (const float *)(planb + P.bcoef);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    auto kern = (op == DD_OP_BPROJ_TW) ? k_fwd<GEOM, 1> : k_fwd<GEOM, 0>;
+    const bool w = (op == DD_OP_BPROJ_TW);
+    auto kern = k_fwd<GEOM, 0, 8>;
+    switch (npass_class(g->num_det)) {
+    case 1: kern = w ? k_fwd<GEOM, 1, 1> : k_fwd<GEOM, 0, 1>; break;
+    case 2: kern = w ? k_fwd<GEOM, 1, 2> : k_fwd<GEOM, 0, 2>; break;
+    case 3: kern = w ? k_fwd<GEOM, 1, 3> : k_fwd<GEOM, 0, 3>; break;
+    case 4: kern = w ? k_fwd<GEOM, 1, 4> : k_fwd<GEOM, 0, 4>; break;
+    default: kern = w ? k_fwd<GEOM, 1, 8> : k_fwd<GEOM, 0, 8>; break;
+    }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);

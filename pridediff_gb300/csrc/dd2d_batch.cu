@@ -198,7 +198,7 @@ __device__ __forceinline__ int next_item(int *counter) {
     return s_item;
 }
 
-template <int GEOM>
+template <int GEOM, int NPASS>
 __global__ void __launch_bounds__(kThreads)
 k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
@@ -229,7 +229,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
         it.taby = tabs + d.taby_off;
         it.out = out + d.sino_off;
         it.sub = sub ? sub + d.sino_off : nullptr;
-        if (!fwd_view<GEOM, 0>(d.g, op, it, smem, Dmax, rsmax, uses)) {
+        if (!fwd_view<GEOM, 0, NPASS>(d.g, op, it, smem, Dmax, rsmax, uses)) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }
@@ -305,7 +305,14 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
                             float *out, const float *sub, int *counter, int *status, int grid,
                             cudaStream_t st) {
     const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax);
-    auto kern = k_fwd_items<GEOM>;
+    auto kern = k_fwd_items<GEOM, 8>;
+    switch (npass_class(L.Dmax)) {
+    case 1: kern = k_fwd_items<GEOM, 1>; break;
+    case 2: kern = k_fwd_items<GEOM, 2>; break;
+    case 3: kern = k_fwd_items<GEOM, 3>; break;
+    case 4: kern = k_fwd_items<GEOM, 4>; break;
+    default: break;
+    }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);

@@ -145,11 +145,19 @@ struct FwdItem {
     const float *sub;            // optional, same layout as out
 };
 
+// Detector passes of a 256-thread CTA (8 warps x 31 bins each) rounded up to
+// the instantiated classes; NPASS sizes the per-thread accumulators, so a
+// smaller class means fewer registers and more resident CTAs per SM.
+__host__ __device__ inline int npass_class(int D) {
+    const int n = (D + kWarps * kBinsPerWarp - 1) / (kWarps * kBinsPerWarp);
+    return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : 8;
+}
+
 // Forward (detector-gather) evaluation of one work item.  The caller has
 // initialised bar[0..1]; `uses` counts completed phases per barrier so that a
 // persistent CTA can run many items back to back.  Returns false if a
 // bounded wait timed out (copies in flight have been drained).
-template <int GEOM, int WEIGHTED>
+template <int GEOM, int WEIGHTED, int NPASS>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, uint32_t *uses) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
@@ -192,7 +200,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     };
 
     const int npass = (D + kWarps * kBinsPerWarp - 1) / (kWarps * kBinsPerWarp);
-    constexpr int kMaxPass = 8;   // D <= 8 * 248 = 1984 detector bins
+    constexpr int kMaxPass = NPASS;   // D <= NPASS * 248 detector bins
     float acc[kMaxPass][kBI];
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++)
@@ -385,9 +393,14 @@ __device__ __forceinline__ void det_index_fan(int geom, const dd_geom2d &g, cons
     *kk = min(max(k, 0), D - 1);
 }
 
+// Detector-table entries per image staged in shared memory for one view
+// (fan beams): the bins a 32x32 tile can touch.  Views whose range is wider
+// gather from global memory instead.
+constexpr int kStage = 256;
+
 // Shared-memory layout of the adjoint kernel (bytes).
 struct AdjSmem {
-    int rec, drec, kd, bar, total;
+    int rec, drec, kd, stage, krange, bar, total;
 };
 
 __host__ __device__ inline AdjSmem adj_smem(int geom) {
@@ -396,12 +409,39 @@ __host__ __device__ inline AdjSmem adj_smem(int geom) {
     s.rec = o; o += 2 * kTile * (int)sizeof(DdLine);
     s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * kTile * (int)sizeof(DdLine);
     s.kd = o; if (geom == DD_GEOM_PARA) o += kWarps * kBI * 32 * (int)sizeof(float);
+    s.stage = o; if (geom != DD_GEOM_PARA) o += 2 * kBI * kStage * (int)sizeof(float2);
+    s.krange = o; o += 4 * (int)sizeof(int);
     s.bar = o; o += 2 * (int)sizeof(uint64_t);
     // the final merge of the two pixel ownerships reuses the record buffers
     const int merge = kBI * kTile * (kTile + 1) * (int)sizeof(float);
     if (o < merge + 16) o = merge + 16;
     s.total = (o + 127) & ~127;
     return s;
+}
+
+// Detector bins [kmin, kmax] that pixels of the tile at (c0, r0) can reach at
+// one view (fan beams): the walked pixel boundaries lie inside the tile's
+// rectangle, whose central projection onto the axis spans the projections of
+// its four corners.  Two bins of margin absorb rounding.
+__device__ __forceinline__ void tile_bin_range(int geom, const dd_geom2d &g, const DdView2 &vw, float view, int c0,
+                                               int r0, int *kmin, int *kmax) {
+    const int W = g.width, H = g.height;
+    const float xs[2] = {((float)c0 - 0.5f * W) * g.pix_x + g.pix_xshift,
+                         ((float)min(c0 + kTile, W) - 0.5f * W) * g.pix_x + g.pix_xshift};
+    const float ys[2] = {(0.5f * H - (float)r0) * g.pix_y + g.pix_yshift,
+                         (0.5f * H - (float)min(r0 + kTile, H)) * g.pix_y + g.pix_yshift};
+    int lo = g.num_det, hi = -1;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float px = xs[i & 1], py = ys[i >> 1];
+        const float u = vw.xb ? dd_map2x(vw.srcx, vw.srcy, px, py) : dd_map2y(vw.srcx, vw.srcy, px, py);
+        int k;
+        det_index_fan(geom, g, vw, view, u, &k);
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+    *kmin = max(lo - 2, 0);
+    *kmax = min(hi + 2, g.num_det - 1);
 }
 
 // Detector-table position of axis value uu (fan beams): bin k with
@@ -457,6 +497,8 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
     DdLine *drecs = reinterpret_cast<DdLine *>(smem + SL.drec);
     float *kdp = reinterpret_cast<float *>(smem + SL.kd);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SL.bar);
+    float2 *stage = reinterpret_cast<float2 *>(smem + SL.stage);
+    int *krange = reinterpret_cast<int *>(smem + SL.krange);   // per buffer: first staged bin, count
     __shared__ int abort_flag;
 
     const int c0 = it.c0, r0 = it.r0;
@@ -470,16 +512,36 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
     __syncthreads();
 
     // records of the tile's lines of view v: rows r0.. (x-branch) or columns c0..
+    // plus, for fan beams, the slice of every image's detector table that the
+    // tile can reach (16-byte aligned: even first bin, even count)
     auto issue = [&](int v, int buf) {
-        const int xbv = views[v].xb;
+        const DdView2 vwv = views[v];
+        const int xbv = vwv.xb;
         const int line0 = xbv ? r0 : c0;
         const int nline = xbv ? H : W;
         const int n = min(kTile, nline - line0);
         const uint32_t bytes = (uint32_t)(n * sizeof(DdLine));
-        dd_mbar_expect_tx(&bar[buf], bytes * (GEOM == DD_GEOM_PARA ? 2u : 1u));
+        uint32_t tx = bytes * (GEOM == DD_GEOM_PARA ? 2u : 1u);
+        int kb = 0, kn = 0;
+        if (GEOM != DD_GEOM_PARA) {
+            int kmin, kmax;
+            tile_bin_range(GEOM, g, vwv, angles[v], c0, r0, &kmin, &kmax);
+            kb = kmin & ~1;
+            kn = (kmax - kb + 2) & ~1;
+            if (kb + kn > rsd) kn = rsd - kb;
+            if (kn > kStage || kn <= 0) kn = 0;
+            tx += (uint32_t)(nb * kn * (int)sizeof(float2));
+        }
+        krange[2 * buf] = kb;
+        krange[2 * buf + 1] = kn;
+        dd_mbar_expect_tx(&bar[buf], tx);
         dd_bulk_g2s(recs + buf * kTile, lines + (size_t)v * nl + line0, bytes, &bar[buf]);
         if (GEOM == DD_GEOM_PARA)
             dd_bulk_g2s(drecs + buf * kTile, dlines + (size_t)v * nl + line0, bytes, &bar[buf]);
+        if (kn > 0)
+            for (int b = 0; b < nb; b++)
+                dd_bulk_g2s(stage + ((size_t)buf * kBI + b) * kStage, dtab + ((size_t)(b0 + b) * V + v) * rsd + kb,
+                            (uint32_t)(kn * sizeof(float2)), &bar[buf]);
     };
 
     float ax[kLinesPerWarp][kBI], ay[kLinesPerWarp][kBI];
@@ -597,15 +659,19 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
                     kL = fan_bin(GEOM, g, vw, view, dpv, ul, idet0, &dkL);
                     offL = ul - dkL;
                 }
+                const int kb = krange[2 * buf], kn = krange[2 * buf + 1];
+                const bool inU = (unsigned)(kU - kb) < (unsigned)kn;
+                const bool inL = (unsigned)(kL - kb) < (unsigned)kn;
+                const float2 *sb = stage + (size_t)buf * kBI * kStage;
 #pragma unroll
                 for (int b = 0; b < kBI; b++) {
                     if (b >= nb) break;
                     const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
-                    const float2 e = __ldg(t + kU);
+                    const float2 e = inU ? sb[b * kStage + (kU - kb)] : __ldg(t + kU);
                     const float hu = fmaf(offU, e.y, e.x);
                     float hl = __shfl_up_sync(0xffffffffu, hu, 1);
                     if (need_low) {
-                        const float2 e2 = __ldg(t + kL);
+                        const float2 e2 = inL ? sb[b * kStage + (kL - kb)] : __ldg(t + kL);
                         hl = fmaf(offL, e2.y, e2.x);
                     }
                     if (valid) {
