@@ -25,6 +25,7 @@
 
 #include "../../include/pridediff_dd.h"
 #include "dd_geom3d.cuh"
+#include "dd_tma.cuh"
 
 namespace dd2 {   // launch accounting and profiling (dd2d.cu)
 struct ProfRec;
@@ -47,21 +48,29 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // ---------------------------------------------------------------------------
 // Layouts
 // ---------------------------------------------------------------------------
+// Per-view tables are padded to 16-byte rows so that one view's row can be
+// moved by a single bulk copy: dp (C+1 column boundaries), mag (C column
+// magnifications), rowz (R x {row0z, row1z}).
 struct PlanLayout {
     size_t views, dp, mag, rowz, linez, lines, total;
-    int nl, nch;
+    int nl, nch, sdp, smag, srz;
 };
+
+__host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
 
 inline PlanLayout plan_layout(const dd_geom3d *g, int V) {
     PlanLayout L;
     const int C = g->num_col, R = g->num_row;
     L.nl = g->height > g->width ? g->height : g->width;
     L.nch = (C + DD3_CHUNK - 1) / DD3_CHUNK;
+    L.sdp = pad4(C + 1);
+    L.smag = pad4(C);
+    L.srz = pad4(2 * R);
     size_t o = 0;
     L.views = o; o = align_up(o + sizeof(DdView3) * (size_t)V, 256);
-    L.dp = o; o = align_up(o + sizeof(float) * (size_t)V * (C + 1), 256);
-    L.mag = o; o = align_up(o + sizeof(float) * (size_t)V * C, 256);
-    L.rowz = o; o = align_up(o + sizeof(float) * 2 * (size_t)V * R, 256);
+    L.dp = o; o = align_up(o + sizeof(float) * (size_t)V * L.sdp, 256);
+    L.mag = o; o = align_up(o + sizeof(float) * (size_t)V * L.smag, 256);
+    L.rowz = o; o = align_up(o + sizeof(float) * (size_t)V * L.srz, 256);
     L.linez = o; o = align_up(o + sizeof(float4) * (size_t)V * L.nl, 256);
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl * L.nch, 256);
     L.total = o;
@@ -110,9 +119,9 @@ __global__ void __launch_bounds__(kThreads) k_views3(dd_geom3d g, const float *_
     }
     __syncthreads();
     const DdView3 w = sw;
-    float *dp = reinterpret_cast<float *>(plan + P.dp) + (size_t)v * (C + 1);
-    float *mag = reinterpret_cast<float *>(plan + P.mag) + (size_t)v * C;
-    float *rz = reinterpret_cast<float *>(plan + P.rowz) + (size_t)v * R * 2;
+    float *dp = reinterpret_cast<float *>(plan + P.dp) + (size_t)v * P.sdp;
+    float *mag = reinterpret_cast<float *>(plan + P.mag) + (size_t)v * P.smag;
+    float *rz = reinterpret_cast<float *>(plan + P.rowz) + (size_t)v * P.srz;
     for (int k = tid; k <= C; k += kThreads) dp[k] = dd3_col_boundary(GEOM, &g, &w, k);
     float mn = 3.0e38f, mx = -3.0e38f;
     for (int k = tid; k < C; k += kThreads) {
@@ -159,7 +168,7 @@ __global__ void __launch_bounds__(128) k_lines3(dd_geom3d g, char *plan, PlanLay
     const int nline = xb ? g.height : g.width;
     if (line >= nline) return;
     const DdView3 w = views[v];
-    const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * (g.num_col + 1);
+    const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * P.sdp;
     DdLine *L = reinterpret_cast<DdLine *>(plan + P.lines) + ((size_t)v * P.nl + line) * P.nch + cc;
     float lz[4];
     dd3_line_setup(GEOM, &g, &w, dp, line, cc, lz, L);
@@ -202,9 +211,9 @@ __global__ void __launch_bounds__(128) k_sino3(dd_geom3d g, const char *__restri
     const DdView3 &w = reinterpret_cast<const DdView3 *>(plan + P.views)[v];
     float scale = w.bp_scale;
     if (FAMILY == 0) {
-        const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * (C + 1);
-        const float *rz = reinterpret_cast<const float *>(plan + P.rowz) + (size_t)v * R * 2;
-        const float mag = reinterpret_cast<const float *>(plan + P.mag)[(size_t)v * C + k];
+        const float *dp = reinterpret_cast<const float *>(plan + P.dp) + (size_t)v * P.sdp;
+        const float *rz = reinterpret_cast<const float *>(plan + P.rowz) + (size_t)v * P.srz;
+        const float mag = reinterpret_cast<const float *>(plan + P.mag)[(size_t)v * P.smag + k];
         float rp0, rp1;
         dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0, &rp1);
         scale = dd3_proj_scale(&g, &w, dp[k], dp[k + 1], rp0, rp1);
@@ -226,34 +235,65 @@ struct Fwd3Args {
     const float *volT;   // (B, Dep, W, H), pixel order reversed along y
     float *out;          // (B, V, R, C)
     const float *sub;    // optional: out = A x - sub
+    int *status;
     int B, V, nrb;
 };
 
 // grid: (view, walk block, row block x volume group); thread = one column of
 // the walk block (8 warps x 32 lanes = 256 columns), kRB rows, kNB volumes.
+// The walk block's column boundaries and magnifications are copied to shared
+// memory once; the record and z quantities of each line are double-buffered
+// in shared memory by bulk copies (TMA) on two mbarriers.
 template <int GEOM, int FAMILY>
 __global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
     const int v = blockIdx.x, cc = blockIdx.y;
     const int rb = blockIdx.z % a.nrb, bg = blockIdx.z / a.nrb;
-    const int kk = threadIdx.x, k = cc * DD3_CHUNK + kk;
-    if (k >= C) return;
+    const int tid = threadIdx.x, kk = tid, c0 = cc * DD3_CHUNK, k = c0 + kk;
+    const int maxn = min(C - c0, DD3_CHUNK);
+    const bool active = kk < maxn;
     const int r0 = rb * kRB, b0 = bg * kNB;
     const int nb = min(kNB, a.B - b0);
     const PlanLayout &P = a.P;
-    const DdView3 w = reinterpret_cast<const DdView3 *>(a.plan + P.views)[v];
-    const float *__restrict__ dp = reinterpret_cast<const float *>(a.plan + P.dp) + (size_t)v * (C + 1);
-    const float *__restrict__ rz = reinterpret_cast<const float *>(a.plan + P.rowz) + (size_t)v * R * 2;
-    const float mag = reinterpret_cast<const float *>(a.plan + P.mag)[(size_t)v * C + k];
+
+    __shared__ __align__(128) DdLine srec[2];
+    __shared__ __align__(16) float4 slz[2];
+    __shared__ float sdp[DD3_CHUNK + 1];
+    __shared__ float smag[DD3_CHUNK];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int abort_flag;
+
+    const float *__restrict__ dpv = reinterpret_cast<const float *>(a.plan + P.dp) + (size_t)v * P.sdp;
+    const float *__restrict__ magv = reinterpret_cast<const float *>(a.plan + P.mag) + (size_t)v * P.smag;
+    const float *__restrict__ rz = reinterpret_cast<const float *>(a.plan + P.rowz) + (size_t)v * P.srz;
     const float4 *__restrict__ linez = reinterpret_cast<const float4 *>(a.plan + P.linez) + (size_t)v * P.nl;
     const DdLine *__restrict__ lines = reinterpret_cast<const DdLine *>(a.plan + P.lines) + (size_t)v * P.nl * P.nch + cc;
+    for (int i = tid; i <= maxn; i += kThreads) sdp[i] = dpv[c0 + i];
+    for (int i = tid; i < maxn; i += kThreads) smag[i] = magv[c0 + i];
+    if (tid == 0) {
+        abort_flag = 0;
+        dd_mbar_init(&bar[0], 1);
+        dd_mbar_init(&bar[1], 1);
+        dd_fence_mbar_init();
+    }
+    __syncthreads();
+
+    const DdView3 w = reinterpret_cast<const DdView3 *>(a.plan + P.views)[v];
+    const int xb = w.xb;
+    const int nline = xb ? H : W, npix = xb ? W : H;
+    auto issue = [&](int line, int buf) {
+        dd_mbar_expect_tx(&bar[buf], (uint32_t)(sizeof(DdLine) + sizeof(float4)));
+        dd_bulk_g2s(&srec[buf], lines + (size_t)line * P.nch, (uint32_t)sizeof(DdLine), &bar[buf]);
+        dd_bulk_g2s(&slz[buf], linez + line, (uint32_t)sizeof(float4), &bar[buf]);
+    };
 
     float rp0[kRB], rp1[kRB];
+    const float mag = active ? smag[kk] : 1.0f;
 #pragma unroll
     for (int q = 0; q < kRB; q++) {
         const int r = r0 + q;
-        if (r < R) {
+        if (active && r < R) {
             dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0[q], &rp1[q]);
         } else {
             rp0[q] = 3.0e38f;    // empty row: the z walk never starts
@@ -266,73 +306,91 @@ __global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
 #pragma unroll
         for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
 
-    const int xb = w.xb;
-    const int nline = xb ? H : W, npix = xb ? W : H;
     const float *__restrict__ src = xb ? a.vol : a.volT;
     const size_t plane = (size_t)nline * npix;
     const size_t vstride = (size_t)Dp * plane;
     src += (size_t)b0 * vstride;
 
+    uint32_t uses[2] = {0u, 0u};
+    int inflight = -1;
+    if (tid == 0) issue(0, 0);
     for (int line = 0; line < nline; line++) {
-        const float4 lz = linez[line];
+        const int buf = line & 1;
+        if (tid == 0 && line + 1 < nline) issue(line + 1, buf ^ 1);
+        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
+        uses[buf]++;
+        __syncthreads();
+        if (abort_flag) {
+            inflight = (line + 1 < nline) ? (buf ^ 1) : -1;
+            break;
+        }
+        const float4 lz = slz[buf];
         bool any = false;
 #pragma unroll
         for (int q = 0; q < kRB; q++) any |= fmaxf(lz.x, rp0[q]) < fminf(lz.y, rp1[q]);
-        if (!any) continue;
-        const DdLine *L = lines + (size_t)line * P.nch;
+        const DdLine *L = &srec[buf];
         DdColWalk cw;
-        if (!dd3_colwalk_init(L, dp, k, kk, &cw)) continue;
-        const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
-        const float *__restrict__ lsrc = src + (size_t)line * npix;
-        bool more = true;
-        while (more) {
-            int js[kNS];
-            float cs[kNS];
-            int n = 0;
+        if (any && dd3_colwalk_init(L, sdp, kk, kk, &cw)) {
+            const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+            const float *__restrict__ lsrc = src + (size_t)line * npix;
+            bool more = true;
+            while (more) {
+                int js[kNS];
+                float cs[kNS];
+                int n = 0;
 #pragma unroll
-            for (int q = 0; q < kNS; q++) {
-                js[q] = 0;
-                cs[q] = 0.0f;
-                if (more) {
-                    int j;
-                    float wd;
-                    if (dd3_colwalk_next(L, &cw, &j, &wd)) {
-                        js[q] = j;
-                        cs[q] = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
-                        n = q + 1;
-                    } else {
-                        more = false;
+                for (int q = 0; q < kNS; q++) {
+                    js[q] = 0;
+                    cs[q] = 0.0f;
+                    if (more) {
+                        int j;
+                        float wd;
+                        if (dd3_colwalk_next(L, &cw, &j, &wd)) {
+                            js[q] = j;
+                            cs[q] = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
+                            n = q + 1;
+                        } else {
+                            more = false;
+                        }
                     }
                 }
-            }
-            if (n == 0) break;
+                if (n == 0) break;
 #pragma unroll
-            for (int q = 0; q < kRB; q++) {
-                DdZ3 z;
-                dd3_zstart(lz.x, lz.y, lz.z, rp0[q], rp1[q], &z);
-                float zw;
-                int s;
-                while (dd3_zstep(&z, lz.z, Dp, &zw, &s)) {
-                    const float *__restrict__ ps = lsrc + (size_t)s * plane;
+                for (int q = 0; q < kRB; q++) {
+                    DdZ3 z;
+                    dd3_zstart(lz.x, lz.y, lz.z, rp0[q], rp1[q], &z);
+                    float zw;
+                    int s;
+                    while (dd3_zstep(&z, lz.z, Dp, &zw, &s)) {
+                        const float *__restrict__ ps = lsrc + (size_t)s * plane;
 #pragma unroll
-                    for (int t = 0; t < kNS; t++) {
-                        if (t < n) {
-                            const float wq = FMUL(zw, cs[t]);
+                        for (int t = 0; t < kNS; t++) {
+                            if (t < n) {
+                                const float wq = FMUL(zw, cs[t]);
 #pragma unroll
-                            for (int b = 0; b < kNB; b++)
-                                if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride + js[t]), acc[q][b]);
+                                for (int b = 0; b < kNB; b++)
+                                    if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride + js[t]), acc[q][b]);
+                            }
                         }
                     }
                 }
             }
         }
+        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
+    if (abort_flag) {
+        // let a copy still in flight land before the CTA exits
+        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
+        if (tid == 0) atomicExch(a.status, DD_ERR_TIMEOUT);
+        return;
+    }
+    if (!active) return;
     const int ko = w.flip ? C - 1 - k : k;
 #pragma unroll
     for (int q = 0; q < kRB; q++) {
         const int r = r0 + q;
         if (r >= R) continue;
-        const float scale = (FAMILY == 0) ? dd3_proj_scale(&g, &w, dp[k], dp[k + 1], rp0[q], rp1[q]) : w.bp_scale;
+        const float scale = (FAMILY == 0) ? dd3_proj_scale(&g, &w, sdp[kk], sdp[kk + 1], rp0[q], rp1[q]) : w.bp_scale;
 #pragma unroll
         for (int b = 0; b < kNB; b++) {
             if (b < nb) {
@@ -356,21 +414,65 @@ struct Adj3Args {
     float *out;          // (B, Dep, H, W)
     const float *base;   // optional: out = base + scale * value (may alias out)
     float scale;
+    int *status;
     int B, V, ntx;
 };
 
+// Shared memory of the adjoint kernel: two buffers of one view's data (the
+// records of the tile's 16 lines in every walk block, the column boundary,
+// column magnification and row tables, the lines' z quantities and the view
+// record), each moved by bulk copies; all sizes are multiples of 16 bytes.
+struct Adj3Smem {
+    int rec, dp, mag, rz, lz, vw, bar, total;
+    uint32_t rec_b, dp_b, mag_b, rz_b, lz_b;
+};
+
+__host__ __device__ inline Adj3Smem adj3_smem(const PlanLayout &P) {
+    Adj3Smem s;
+    s.rec_b = (uint32_t)(kTile * P.nch * sizeof(DdLine));
+    s.dp_b = (uint32_t)(P.sdp * sizeof(float));
+    s.mag_b = (uint32_t)(P.smag * sizeof(float));
+    s.rz_b = (uint32_t)(P.srz * sizeof(float));
+    s.lz_b = (uint32_t)(kTile * sizeof(float4));
+    int o = 0;
+    s.rec = o; o += 2 * (int)s.rec_b;
+    s.dp = o; o += 2 * (int)s.dp_b;
+    s.mag = o; o += 2 * (int)s.mag_b;
+    s.rz = o; o += 2 * (int)s.rz_b;
+    s.lz = o; o += 2 * (int)s.lz_b;
+    s.vw = o; o += 2 * (int)sizeof(DdView3);
+    s.bar = o; o += 2 * (int)sizeof(uint64_t);
+    s.total = (o + 127) & ~127;
+    return s;
+}
+
+// Can view w see the slab of slices [s0, s0 + kZS) on the walked lines
+// l0..l1 (with one slice of margin)?
+__device__ __forceinline__ bool slab_visible(const dd_geom3d &g, const DdView3 &w, int l0, int l1, int s0,
+                                             float zr0, float zr1) {
+    const float m0 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l0));
+    const float m1 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l1));
+    const float zsA = w.z0 + (float)(s0 - 1) * g.pix_z, zsB = w.z0 + (float)(s0 + kZS + 1) * g.pix_z;
+    return dd3_slab_lit(&w, fminf(m0, m1), fmaxf(m0, m1), zsA, zsB, zr0, zr1);
+}
+
 // grid: (voxel-column tile, slab of kZS slices, volume group); thread = one
-// (x, y) voxel column of a 16 x 16 tile.
+// (x, y) voxel column of a 16 x 16 tile.  Views whose detector cannot see the
+// slab are skipped when their copy would be issued.
 template <int GEOM, int FAMILY>
 __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
+    extern __shared__ __align__(128) unsigned char sm[];
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
+    const PlanLayout &P = a.P;
+    const Adj3Smem S = adj3_smem(P);
+    const int tid = threadIdx.x;
     const int tX = blockIdx.x % a.ntx, tY = blockIdx.x / a.ntx;
-    const int x = tX * kTile + (threadIdx.x & (kTile - 1)), y = tY * kTile + (threadIdx.x / kTile);
-    if (x >= W || y >= H) return;
+    const int xlo = tX * kTile, ylo = tY * kTile;
+    const int x = xlo + (tid & (kTile - 1)), y = ylo + (tid / kTile);
+    const bool active = x < W && y < H;
     const int s0 = blockIdx.y * kZS, b0 = blockIdx.z * kNB;
     const int nb = min(kNB, a.B - b0);
-    const PlanLayout &P = a.P;
     const DdView3 *__restrict__ views = reinterpret_cast<const DdView3 *>(a.plan + P.views);
     const float *__restrict__ dpt = reinterpret_cast<const float *>(a.plan + P.dp);
     const float *__restrict__ magt = reinterpret_cast<const float *>(a.plan + P.mag);
@@ -379,9 +481,39 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
     const DdLine *__restrict__ lines = reinterpret_cast<const DdLine *>(a.plan + P.lines);
     const size_t per = (size_t)a.V * R * C;
     const float *__restrict__ ssb = a.ss + (size_t)b0 * per;
-    // line ranges of this CTA (for the slab visibility test)
-    const int xlo = tX * kTile, xhi = min(xlo + kTile - 1, W - 1);
-    const int ylo = tY * kTile, yhi = min(ylo + kTile - 1, H - 1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + S.bar);
+    __shared__ int abort_flag;
+    __shared__ int seen[2];   // per buffer: 1 if the view sees the slab (data copied)
+
+    if (tid == 0) {
+        abort_flag = 0;
+        dd_mbar_init(&bar[0], 1);
+        dd_mbar_init(&bar[1], 1);
+        dd_fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int v, int buf) {
+        const DdView3 wv = views[v];
+        const int xbv = wv.xb;
+        const int l0 = xbv ? ylo : xlo;
+        const int n = min(kTile, (xbv ? H : W) - l0);
+        const float *rzv = rzt + (size_t)v * P.srz;
+        const bool lit = slab_visible(g, wv, l0, l0 + n - 1, s0, rzv[0], rzv[2 * R - 1]);
+        seen[buf] = lit ? 1 : 0;
+        if (!lit) {
+            dd_mbar_expect_tx(&bar[buf], 0u);   // completes the phase with no data
+            return;
+        }
+        const uint32_t rb = (uint32_t)(n * P.nch * sizeof(DdLine)), lb = (uint32_t)(n * sizeof(float4));
+        dd_mbar_expect_tx(&bar[buf], rb + S.dp_b + S.mag_b + S.rz_b + lb + (uint32_t)sizeof(DdView3));
+        dd_bulk_g2s(sm + S.rec + buf * S.rec_b, lines + ((size_t)v * P.nl + l0) * P.nch, rb, &bar[buf]);
+        dd_bulk_g2s(sm + S.dp + buf * S.dp_b, dpt + (size_t)v * P.sdp, S.dp_b, &bar[buf]);
+        dd_bulk_g2s(sm + S.mag + buf * S.mag_b, magt + (size_t)v * P.smag, S.mag_b, &bar[buf]);
+        dd_bulk_g2s(sm + S.rz + buf * S.rz_b, rzv, S.rz_b, &bar[buf]);
+        dd_bulk_g2s(sm + S.lz + buf * S.lz_b, linez + (size_t)v * P.nl + l0, lb, &bar[buf]);
+        dd_bulk_g2s(sm + S.vw + buf * (int)sizeof(DdView3), views + v, (uint32_t)sizeof(DdView3), &bar[buf]);
+    };
 
     float acc[kZS][kNB];
 #pragma unroll
@@ -389,56 +521,73 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
 #pragma unroll
         for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
 
+    uint32_t uses[2] = {0u, 0u};
+    int inflight = -1;
+    if (tid == 0) issue(0, 0);
     for (int v = 0; v < a.V; v++) {
-        const DdView3 w = views[v];
-        const float *__restrict__ rz = rzt + (size_t)v * R * 2;
-        {   // can this view see the slab at all?
-            const int l0 = w.xb ? ylo : xlo, l1 = w.xb ? yhi : xhi;
-            const float m0 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l0));
-            const float m1 = dd3_line_mag(&w, dd3_line_pos(&g, &w, l1));
-            const float zsA = w.z0 + (float)(s0 - 1) * g.pix_z, zsB = w.z0 + (float)(s0 + kZS + 1) * g.pix_z;
-            if (!dd3_slab_lit(&w, fminf(m0, m1), fmaxf(m0, m1), zsA, zsB, rz[0], rz[2 * R - 1])) continue;
+        const int buf = v & 1;
+        if (tid == 0 && v + 1 < a.V) issue(v + 1, buf ^ 1);
+        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
+        uses[buf]++;
+        __syncthreads();
+        if (abort_flag) {
+            inflight = (v + 1 < a.V) ? (buf ^ 1) : -1;
+            break;
         }
-        const int line = w.xb ? y : x;
-        const int j = w.xb ? x : H - 1 - y;
-        const float4 lz = linez[(size_t)v * P.nl + line];
-        const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
-        const float margin = 0.25f * fabsf(lz.z);
-        const float *__restrict__ dp = dpt + (size_t)v * (C + 1);
-        const DdLine *__restrict__ lrec = lines + ((size_t)v * P.nl + line) * P.nch;
-        const float *__restrict__ ssv = ssb + (size_t)v * R * C;
-        for (int cc = 0; cc < P.nch; cc++) {
-            DdPixWalk pw;
-            if (!dd3_pixwalk_init(GEOM, &g, &w, lrec + cc, dp, cc, j, &pw)) continue;
-            int k;
-            float wd;
-            while (dd3_pixwalk_next(dp, &pw, &k, &wd)) {
-                const float coef = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
-                const float mag = magt[(size_t)v * C + k];
-                const float *__restrict__ ssk = ssv + k;
+        if (active && seen[buf]) {
+            const DdView3 &w = *reinterpret_cast<const DdView3 *>(sm + S.vw + buf * (int)sizeof(DdView3));
+            const float *dp = reinterpret_cast<const float *>(sm + S.dp + buf * S.dp_b);
+            const float *mg = reinterpret_cast<const float *>(sm + S.mag + buf * S.mag_b);
+            const float *rz = reinterpret_cast<const float *>(sm + S.rz + buf * S.rz_b);
+            const int xb = w.xb;
+            const int rl = xb ? (y - ylo) : (x - xlo);
+            const int line = (xb ? ylo : xlo) + rl;
+            const int j = xb ? x : H - 1 - y;
+            const float4 lz = reinterpret_cast<const float4 *>(sm + S.lz + buf * S.lz_b)[rl];
+            const DdLine *lrec = reinterpret_cast<const DdLine *>(sm + S.rec + buf * S.rec_b) + rl * P.nch;
+            const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+            const float margin = 0.25f * fabsf(lz.z);
+            const float *__restrict__ ssv = ssb + (size_t)v * R * C;
+            for (int cc = 0; cc < P.nch; cc++) {
+                DdPixWalk pw;
+                if (!dd3_pixwalk_init(GEOM, &g, &w, lrec + cc, dp, cc, j, &pw)) continue;
+                int k;
+                float wd;
+                while (dd3_pixwalk_next(dp, &pw, &k, &wd)) {
+                    const float coef = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
+                    const float mag = mg[k];
+                    const float *__restrict__ ssk = ssv + k;
 #pragma unroll
-                for (int q = 0; q < kZS; q++) {
-                    const int s = s0 + q;
-                    if (s < Dp) {
-                        const float zlo = FADD(lz.x, FMUL((float)s, lz.z));
-                        const float zhi = FADD(zlo, lz.z);
-                        for (int r = dd3_row_first(GEOM, &w, rz, R, mag, zlo, margin); r < R; r++) {
-                            float e0, e1;
-                            dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &e0, &e1);
-                            if (e0 >= zhi + margin) break;
-                            const float zw = dd3_zweight(lz.x, lz.y, lz.z, e0, e1, s, Dp);
-                            if (zw != 0.0f) {
-                                const float wq = FMUL(zw, coef);
+                    for (int q = 0; q < kZS; q++) {
+                        const int s = s0 + q;
+                        if (s < Dp) {
+                            const float zlo = FADD(lz.x, FMUL((float)s, lz.z));
+                            const float zhi = FADD(zlo, lz.z);
+                            for (int r = dd3_row_first(GEOM, &w, rz, R, mag, zlo, margin); r < R; r++) {
+                                float e0, e1;
+                                dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &e0, &e1);
+                                if (e0 >= zhi + margin) break;
+                                const float zw = dd3_zweight(lz.x, lz.y, lz.z, e0, e1, s, Dp);
+                                if (zw != 0.0f) {
+                                    const float wq = FMUL(zw, coef);
 #pragma unroll
-                                for (int b = 0; b < kNB; b++)
-                                    if (b < nb) acc[q][b] = fmaf(wq, __ldg(ssk + (size_t)b * per + (size_t)r * C), acc[q][b]);
+                                    for (int b = 0; b < kNB; b++)
+                                        if (b < nb) acc[q][b] = fmaf(wq, __ldg(ssk + (size_t)b * per + (size_t)r * C), acc[q][b]);
+                                }
                             }
                         }
                     }
                 }
             }
         }
+        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
+    if (abort_flag) {
+        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
+        if (tid == 0) atomicExch(a.status, DD_ERR_TIMEOUT);
+        return;
+    }
+    if (!active) return;
 #pragma unroll
     for (int q = 0; q < kZS; q++) {
         const int s = s0 + q;
@@ -480,6 +629,8 @@ int validate(int scan, int op, const dd_geom3d *g, int B, int V) {
     if ((long long)V * g->num_row * g->num_col * B > lim) return DD_ERR_SIZE_OVERFLOW;
     if (g->width > 8192 || g->height > 8192 || V > 65535 || g->num_row > 65535 || g->num_col > 65535)
         return DD_ERR_SIZE_OVERFLOW;
+    // one view's staged data (two buffers) must fit the adjoint's shared memory
+    if (adj3_smem(plan_layout(g, V)).total > 200 * 1024) return DD_ERR_SIZE_OVERFLOW;
     return DD_OK;
 }
 
@@ -524,6 +675,15 @@ int launch_fwd(int family, const Fwd3Args &a, cudaStream_t st) {
     return launch_status();
 }
 
+template <int GEOM, int FAMILY>
+int launch_adj_kernel(const Adj3Args &a, const dim3 &grid, cudaStream_t st) {
+    const int smem = adj3_smem(a.P).total;
+    if (cudaFuncSetAttribute(k_adj3<GEOM, FAMILY>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    k_adj3<GEOM, FAMILY><<<grid, kThreads, smem, st>>>(a);
+    return DD_OK;
+}
+
 template <int GEOM>
 int launch_adj(int family, const Adj3Args &a, const float *in, float *ss, cudaStream_t st) {
     const dd_geom3d &g = a.g;
@@ -535,10 +695,12 @@ int launch_adj(int family, const Adj3Args &a, const float *in, float *ss, cudaSt
     const int nty = (g.height + kTile - 1) / kTile;
     const dim3 grid((unsigned)(a.ntx * nty), (unsigned)((g.depth + kZS - 1) / kZS), (unsigned)((a.B + kNB - 1) / kNB));
     dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_ADJOINT, st);
-    if (family == 0) k_adj3<GEOM, 0><<<grid, kThreads, 0, st>>>(a);
-    else if (family == 1) k_adj3<GEOM, 1><<<grid, kThreads, 0, st>>>(a);
-    else k_adj3<GEOM, 2><<<grid, kThreads, 0, st>>>(a);
+    int rc;
+    if (family == 0) rc = launch_adj_kernel<GEOM, 0>(a, grid, st);
+    else if (family == 1) rc = launch_adj_kernel<GEOM, 1>(a, grid, st);
+    else rc = launch_adj_kernel<GEOM, 2>(a, grid, st);
     dd2::prof_end(pr, st);
+    if (rc != DD_OK) return rc;
     dd2::count_launches(2);
     return launch_status();
 }
@@ -556,10 +718,12 @@ int transpose(const dd_geom3d *g, const float *in, float *out, int B, cudaStream
 
 // Forward-type operator into `out` (optionally minus `sub`).
 int forward(int scan, int op, const dd_geom3d *g, const char *planb, const float *in, float *out,
-            const float *sub, int B, int V, char *volT, cudaStream_t st) {
+            const float *sub, int B, int V, char *volT, int *status, cudaStream_t st) {
     const int s1 = transpose(g, in, (float *)volT, B, st);
     if (s1 != DD_OK) return s1;
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
     Fwd3Args a;
+    a.status = status;
     a.g = *g;
     a.plan = planb;
     a.P = plan_layout(g, V);
@@ -578,8 +742,10 @@ int forward(int scan, int op, const dd_geom3d *g, const char *planb, const float
 
 // Adjoint-type operator: out = value, or out = base + scale * value.
 int adjoint(int scan, int op, const dd_geom3d *g, const char *planb, const float *in, float *out,
-            const float *basep, float scale, int B, int V, char *ss, cudaStream_t st) {
+            const float *basep, float scale, int B, int V, char *ss, int *status, cudaStream_t st) {
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
     Adj3Args a;
+    a.status = status;
     a.g = *g;
     a.plan = planb;
     a.P = plan_layout(g, V);
@@ -638,8 +804,9 @@ extern "C" int dd3d_apply_planned(int scan, int op, const dd_geom3d *g, const vo
     if (!workspace || workspace_bytes < A.total) return DD_ERR_WORKSPACE;
     char *wb = (char *)workspace;
     cudaStream_t s = (cudaStream_t)stream;
-    if (f) return forward(scan, op, g, (const char *)planp, in, out, nullptr, batch, num_view, wb + A.volT, s);
-    return adjoint(scan, op, g, (const char *)planp, in, out, nullptr, 0.0f, batch, num_view, wb + A.ss, s);
+    int *status = (int *)(wb + A.status);
+    if (f) return forward(scan, op, g, (const char *)planp, in, out, nullptr, batch, num_view, wb + A.volT, status, s);
+    return adjoint(scan, op, g, (const char *)planp, in, out, nullptr, 0.0f, batch, num_view, wb + A.ss, status, s);
 }
 
 extern "C" size_t dd3d_workspace_bytes(int scan, int op, const dd_geom3d *g, int batch, int num_view) {
@@ -678,9 +845,10 @@ extern "C" int dd3d_dc_step(int scan, const dd_geom3d *g, const void *planp, flo
     char *wb = (char *)workspace;
     cudaStream_t s = (cudaStream_t)stream;
     const char *pb = (const char *)planp;
-    const int s1 = forward(scan, DD_OP_PROJ, g, pb, x, resid, y, batch, num_view, wb + A.volT, s);
+    int *status = (int *)(wb + A.status);
+    const int s1 = forward(scan, DD_OP_PROJ, g, pb, x, resid, y, batch, num_view, wb + A.volT, status, s);
     if (s1 != DD_OK) return s1;
-    return adjoint(scan, DD_OP_PROJ_T, g, pb, resid, x, x, -eta, batch, num_view, wb + A.ss, s);
+    return adjoint(scan, DD_OP_PROJ_T, g, pb, resid, x, x, -eta, batch, num_view, wb + A.ss, status + 1, s);
 }
 
 // named entries (RadonTorch.cpp:1395-1414)

@@ -290,4 +290,10 @@ DD_HD float dd_cw_arc(float sx, float sy, float px, float py) {
 }
 // floor() of a float expression evaluated as the reference does (the FP32
 // quotient is promoted to double before flooring).
-DD_HD int dd_ifloor(float q) { return (int)floor((double)q); }
+DD_HD int dd_ifloor(float q) {
+#if defined(__CUDA_ARCH__)
+    return (int)floorf(q);   // same value as the double floor for every float
+#else
+    return (int)floor((double)q);
+#endif
+}

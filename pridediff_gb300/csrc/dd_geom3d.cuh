@@ -46,12 +46,41 @@ struct DdView3 {
     float z0, z1;         // volume extent in z
     float magmin, magmax; // range of the per-column row magnification
     float rzA, rzB;       // row0z(r) ~= rzA + r * rzB (row candidate search)
-    float pad[4];
+    float pad[6];
 };
+// the view record and the line record are moved by bulk copies: sizes must be
+// multiples of 16 bytes (and arrays of them keep every element 16-byte aligned)
+static_assert(sizeof(DdView3) == 128, "DdView3 must be 128 bytes");
+static_assert(sizeof(DdLine) % 16 == 0, "DdLine must be a multiple of 16 bytes");
 
 // Per-(view, line) z quantities: p0z, p1z (volume z extent on the line's
 // plane), pintz (slice pitch there), parea (pixel area for the DD-BP family).
 // Stored as float4 {p0z, p1z, pintz, parea}.
+
+// floor of the correctly rounded quotient num / den, as the reference's
+// FP32 walk computes it.  On the device an approximate quotient settles
+// every case that is not within a few ulp of an integer (where the rounded
+// and the approximate quotient must have the same floor); the remaining
+// cases take the correctly rounded division.
+DD_HD int dd3_floor_div(float num, float den) {
+#if defined(__CUDA_ARCH__)
+    if (fabsf(den) < 1.0e30f) {
+        const float q = __fdividef(num, den);
+        const float n = rintf(q);
+        if (fabsf(q - n) > 1.0e-6f * fmaxf(1.0f, fabsf(q)) && fabsf(q) < 1.0e9f) return (int)floorf(q);
+    }
+#endif
+    return dd_ifloor(FDIV(num, den));
+}
+
+// Approximate quotient for estimates that are corrected afterwards.
+DD_HD float dd3_approx_div(float num, float den) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(num, den);
+#else
+    return num / den;
+#endif
+}
 
 // ---------------------------------------------------------------------------
 // View set-up: ConeFlatDisCUDA3d.cu:62-105, ConeArcDisCUDA3d.cu:40-60,
@@ -109,7 +138,7 @@ DD_HD void dd3_view_scalars(int geom, const dd_geom3d *g, float view, const floa
     w->z1 = (float)DADD(DMUL(Dp / 2.0, (double)g->pix_z), pzs);
     w->magmin = w->magmax = 1.0f;
     w->rzA = w->rzB = 0.0f;
-    for (int i = 0; i < 4; i++) w->pad[i] = 0.0f;
+    for (int i = 0; i < 6; i++) w->pad[i] = 0.0f;
 }
 
 // Sorted column boundary k (0..C) on the projection axis.
@@ -380,7 +409,7 @@ struct DdZ3 {
 DD_HD void dd3_zstart(float p0z, float p1z, float pintz, float rp0, float rp1, DdZ3 *z) {
     z->bz0 = p0z > rp0 ? p0z : rp0;
     z->bz1 = p1z < rp1 ? p1z : rp1;
-    z->is = (z->bz0 == p0z) ? 0 : dd_ifloor(FDIV(FSUB(z->bz0, p0z), pintz));
+    z->is = (z->bz0 == p0z) ? 0 : dd3_floor_div(FSUB(z->bz0, p0z), pintz);
     z->pz1 = FADD(FMUL((float)(z->is + 1), pintz), p0z);
 }
 
@@ -421,14 +450,15 @@ DD_HD int dd3_col_of(int geom, const dd_geom3d *g, const DdView3 *w, const float
     float kf;
     if (geom == DD_GEOM3_CONE_FLAT) {
         const float R = g->iso_source;
-        const float t = w->xb ? R * u * w->c / (R + u * w->s) : R * u * w->s / (R - u * w->c);
-        const float q = (t - w->vbs) / w->vds;
+        const float t = w->xb ? dd3_approx_div(R * u * w->c, R + u * w->s) : dd3_approx_div(R * u * w->s, R - u * w->c);
+        const float q = dd3_approx_div(t - w->vbs, w->vds);
         kf = w->flip ? (float)C * 0.5f - q : q + (float)C * 0.5f;
     } else {
-        float ang = w->xb ? atan2f(u - w->srcx, w->srcy) : 1.5707963267948966f - atanf((u - w->srcy) / w->srcx);
+        float ang = w->xb ? atan2f(u - w->srcx, w->srcy)
+                          : 1.5707963267948966f - atanf(dd3_approx_div(u - w->srcy, w->srcx));
         const float base = w->view + w->colshift;
         ang += 3.14159265358979f * rintf((base - ang) * 0.3183098861837907f);
-        const float q = (ang - base) / w->colsz;
+        const float q = dd3_approx_div(ang - base, w->colsz);
         kf = w->flip ? (float)C * 0.5f - q : q + (float)C * 0.5f;
     }
     int k = klo;
@@ -571,10 +601,11 @@ DD_HD float dd3_coef(int geom, int family, const dd_geom3d *g, const DdView3 *w,
 // walk rows upward until the lower boundary passes the slice top.
 DD_HD int dd3_row_first(int geom, const DdView3 *w, const float *rowz, int R, float mag, float zlo,
                         float margin) {
-    const float zeta = (geom == DD_GEOM3_SPIRAL) ? (zlo - w->srcz) / mag + w->srcz : zlo / mag;
+    const float zeta = (geom == DD_GEOM3_SPIRAL) ? dd3_approx_div(zlo - w->srcz, mag) + w->srcz
+                                                 : dd3_approx_div(zlo, mag);
     int r = 0;
     if (w->rzB > 0.0f) {
-        const float rf = (zeta - w->rzA) / w->rzB;
+        const float rf = dd3_approx_div(zeta - w->rzA, w->rzB);
         if (rf == rf) r = (int)floorf(fminf(fmaxf(rf, -1.0f), (float)R)) - 1;
     }
     if (r < 0) r = 0;
