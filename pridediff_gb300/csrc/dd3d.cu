@@ -37,11 +37,10 @@ void count_launches(int n);
 namespace dd3 {
 
 constexpr int kThreads = 256;
-constexpr int kRB = 8;     // detector rows per forward thread
 constexpr int kNB = 2;     // volumes per thread
-constexpr int kNS = 4;     // column segments held in registers per pass
 constexpr int kTile = 16;  // adjoint: 16 x 16 voxel columns per CTA
 constexpr int kZS = 8;     // adjoint: slices per thread
+constexpr int kWarps3 = kThreads / 32;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -227,6 +226,10 @@ __global__ void __launch_bounds__(128) k_sino3(dd_geom3d g, const char *__restri
 // ---------------------------------------------------------------------------
 // Forward-type kernel: detector gathers
 // ---------------------------------------------------------------------------
+constexpr int kFC = 32;    // detector columns per CTA (the lanes of a warp)
+constexpr int kFR = 8;     // consecutive detector rows per thread; 8 warps -> 64 rows per CTA
+constexpr int kSeg = 8;    // column segments of one line held in shared memory
+
 struct Fwd3Args {
     dd_geom3d g;
     const char *plan;
@@ -239,70 +242,106 @@ struct Fwd3Args {
     int B, V, nrb;
 };
 
-// grid: (view, walk block, row block x volume group); thread = one column of
-// the walk block (8 warps x 32 lanes = 256 columns), kRB rows, kNB volumes.
-// The walk block's column boundaries and magnifications are copied to shared
-// memory once; the record and z quantities of each line are double-buffered
-// in shared memory by bulk copies (TMA) on two mbarriers.
+// grid: (view, group of 32 columns inside one walk block, row block x volume
+// group).  Lane = column, warp w = rows r0 + 8w .. r0 + 8w + 7, kNB volumes.
+// The overlap segments of a line (pixel, width x operator factor) depend on
+// the column only, so they are computed once per line and column -- by one
+// warp, in rotation, one line ahead -- into shared memory, and reused by all
+// 64 rows.  Line records arrive by bulk copies (TMA) two lines ahead.
 template <int GEOM, int FAMILY>
 __global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
-    const int v = blockIdx.x, cc = blockIdx.y;
+    const int v = blockIdx.x, cg = blockIdx.y;
     const int rb = blockIdx.z % a.nrb, bg = blockIdx.z / a.nrb;
-    const int tid = threadIdx.x, kk = tid, c0 = cc * DD3_CHUNK, k = c0 + kk;
-    const int maxn = min(C - c0, DD3_CHUNK);
-    const bool active = kk < maxn;
-    const int r0 = rb * kRB, b0 = bg * kNB;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int cc = (cg * kFC) / DD3_CHUNK, c0 = cc * DD3_CHUNK;
+    const int k = cg * kFC + lane, kk = k - c0;
+    const bool active = k < C;
+    const int r0 = rb * (kFR * kWarps3) + warp * kFR, b0 = bg * kNB;
     const int nb = min(kNB, a.B - b0);
     const PlanLayout &P = a.P;
 
     __shared__ __align__(128) DdLine srec[2];
-    __shared__ __align__(16) float4 slz[2];
-    __shared__ float sdp[DD3_CHUNK + 1];
-    __shared__ float smag[DD3_CHUNK];
+    __shared__ __align__(16) float4 slzr[2];        // z quantities arriving with each record
+    __shared__ __align__(16) float4 slz[2];         // z quantities of the segment buffers
+    __shared__ int segj[2][kSeg][kFC];
+    __shared__ float segc[2][kSeg][kFC];
+    __shared__ int segn[2][kFC];
+    __shared__ float sdp[kFC + 1];
     __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int abort_flag;
+    __shared__ int abort_flag, nissue[2], nwait[2];   // copies issued / waited per record buffer
 
+    const DdView3 w = reinterpret_cast<const DdView3 *>(a.plan + P.views)[v];
     const float *__restrict__ dpv = reinterpret_cast<const float *>(a.plan + P.dp) + (size_t)v * P.sdp;
-    const float *__restrict__ magv = reinterpret_cast<const float *>(a.plan + P.mag) + (size_t)v * P.smag;
     const float *__restrict__ rz = reinterpret_cast<const float *>(a.plan + P.rowz) + (size_t)v * P.srz;
     const float4 *__restrict__ linez = reinterpret_cast<const float4 *>(a.plan + P.linez) + (size_t)v * P.nl;
     const DdLine *__restrict__ lines = reinterpret_cast<const DdLine *>(a.plan + P.lines) + (size_t)v * P.nl * P.nch + cc;
-    for (int i = tid; i <= maxn; i += kThreads) sdp[i] = dpv[c0 + i];
-    for (int i = tid; i < maxn; i += kThreads) smag[i] = magv[c0 + i];
+    if (tid <= kFC) sdp[tid] = dpv[min(cg * kFC + tid, C)];
     if (tid == 0) {
         abort_flag = 0;
+        nissue[0] = nissue[1] = nwait[0] = nwait[1] = 0;
         dd_mbar_init(&bar[0], 1);
         dd_mbar_init(&bar[1], 1);
         dd_fence_mbar_init();
     }
     __syncthreads();
 
-    const DdView3 w = reinterpret_cast<const DdView3 *>(a.plan + P.views)[v];
     const int xb = w.xb;
     const int nline = xb ? H : W, npix = xb ? W : H;
     auto issue = [&](int line, int buf) {
+        nissue[buf]++;
         dd_mbar_expect_tx(&bar[buf], (uint32_t)(sizeof(DdLine) + sizeof(float4)));
         dd_bulk_g2s(&srec[buf], lines + (size_t)line * P.nch, (uint32_t)sizeof(DdLine), &bar[buf]);
-        dd_bulk_g2s(&slz[buf], linez + line, (uint32_t)sizeof(float4), &bar[buf]);
+        dd_bulk_g2s(&slzr[buf], linez + line, (uint32_t)sizeof(float4), &bar[buf]);
+    };
+    // segments of line m (record buffer m & 1) into segment buffer sb; one warp
+    auto produce = [&](int m, int sb) -> bool {
+        const int rbuf = m & 1;
+        const uint32_t parity = (uint32_t)nwait[rbuf] & 1u;
+        if (!dd_mbar_wait(&bar[rbuf], parity)) return false;
+        const DdLine *L = &srec[rbuf];
+        const float4 lz = slzr[rbuf];
+        if (lane == 0) slz[sb] = lz;
+        int n = 0;
+        DdColWalk cw;
+        if (active && dd3_colwalk_init(L, sdp, lane, kk, &cw)) {
+            const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, m) : 0.0f;
+            int j;
+            float wd;
+            while (dd3_colwalk_next(L, &cw, &j, &wd)) {
+                if (n == kSeg) {   // more than kSeg segments: consumers walk the record themselves
+                    n = kSeg + 1;
+                    break;
+                }
+                segj[sb][n][lane] = j;
+                segc[sb][n][lane] = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
+                n++;
+            }
+        }
+        segn[sb][lane] = n;
+        __syncwarp();
+        if (lane == 0) nwait[rbuf]++;
+        return true;
     };
 
-    float rp0[kRB], rp1[kRB];
-    const float mag = active ? smag[kk] : 1.0f;
+    float rp0[kFR], rp1[kFR];
+    {
+        const float mag = active ? reinterpret_cast<const float *>(a.plan + P.mag)[(size_t)v * P.smag + k] : 1.0f;
 #pragma unroll
-    for (int q = 0; q < kRB; q++) {
-        const int r = r0 + q;
-        if (active && r < R) {
-            dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0[q], &rp1[q]);
-        } else {
-            rp0[q] = 3.0e38f;    // empty row: the z walk never starts
-            rp1[q] = -3.0e38f;
+        for (int q = 0; q < kFR; q++) {
+            const int r = r0 + q;
+            if (active && r < R) {
+                dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0[q], &rp1[q]);
+            } else {
+                rp0[q] = 3.0e38f;    // empty row: the z walk never starts
+                rp1[q] = -3.0e38f;
+            }
         }
     }
-    float acc[kRB][kNB];
+    float acc[kFR][kNB];
 #pragma unroll
-    for (int q = 0; q < kRB; q++)
+    for (int q = 0; q < kFR; q++)
 #pragma unroll
         for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
 
@@ -311,86 +350,97 @@ __global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
     const size_t vstride = (size_t)Dp * plane;
     src += (size_t)b0 * vstride;
 
-    uint32_t uses[2] = {0u, 0u};
-    int inflight = -1;
-    if (tid == 0) issue(0, 0);
-    for (int line = 0; line < nline; line++) {
-        const int buf = line & 1;
-        if (tid == 0 && line + 1 < nline) issue(line + 1, buf ^ 1);
-        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
-        uses[buf]++;
-        __syncthreads();
-        if (abort_flag) {
-            inflight = (line + 1 < nline) ? (buf ^ 1) : -1;
-            break;
-        }
-        const float4 lz = slz[buf];
-        bool any = false;
-#pragma unroll
-        for (int q = 0; q < kRB; q++) any |= fmaxf(lz.x, rp0[q]) < fminf(lz.y, rp1[q]);
-        const DdLine *L = &srec[buf];
-        DdColWalk cw;
-        if (any && dd3_colwalk_init(L, sdp, kk, kk, &cw)) {
-            const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+    // prologue: records 0 and 1 in flight, segments of line 0 computed
+    if (tid == 0) {
+        issue(0, 0);
+        if (nline > 1) issue(1, 1);
+    }
+    __syncthreads();
+    if (warp == 0 && !produce(0, 0)) abort_flag = 1;
+    __syncthreads();
+    if (tid == 0 && !abort_flag && nline > 2) issue(2, 0);
+    for (int line = 0; line < nline && !abort_flag; line++) {
+        const int sb = line & 1;
+        if (line + 1 < nline && warp == (line & (kWarps3 - 1)) && !produce(line + 1, sb ^ 1)) abort_flag = 1;
+        // consume line `line`
+        const int n = segn[sb][lane];
+        if (active && n > 0) {
+            const float4 lz = slz[sb];
             const float *__restrict__ lsrc = src + (size_t)line * npix;
-            bool more = true;
-            while (more) {
-                int js[kNS];
-                float cs[kNS];
-                int n = 0;
+            if (n <= kSeg) {
 #pragma unroll
-                for (int q = 0; q < kNS; q++) {
-                    js[q] = 0;
-                    cs[q] = 0.0f;
-                    if (more) {
-                        int j;
-                        float wd;
-                        if (dd3_colwalk_next(L, &cw, &j, &wd)) {
-                            js[q] = j;
-                            cs[q] = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
-                            n = q + 1;
-                        } else {
-                            more = false;
+                for (int q = 0; q < kFR; q++) {
+                    const float bz0 = fmaxf(lz.x, rp0[q]), bz1 = fminf(lz.y, rp1[q]);
+                    if (!(bz0 < bz1)) continue;
+                    int s = dd3_slice_first(bz0, lz.x, lz.z);
+                    float zhi = dd3_zb(lz.x, lz.z, s);
+                    for (; s < Dp; s++) {
+                        const float zlo = zhi;
+                        if (!(zlo < bz1)) break;
+                        zhi = dd3_zb(lz.x, lz.z, s + 1);
+                        const float zw = dd3_cell(bz0, bz1, zlo, zhi);
+                        if (!(zw > 0.0f)) continue;
+                        const float *__restrict__ ps = lsrc + (size_t)s * plane;
+                        for (int t = 0; t < n; t++) {
+                            const float wq = FMUL(zw, segc[sb][t][lane]);
+                            const int j = segj[sb][t][lane];
+#pragma unroll
+                            for (int b = 0; b < kNB; b++)
+                                if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride + j), acc[q][b]);
                         }
                     }
                 }
-                if (n == 0) break;
+            } else {
+                // wide column: walk the record in global memory
+                const DdLine *Lg = lines + (size_t)line * P.nch;
+                const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
+                DdColWalk cw;
+                if (dd3_colwalk_init(Lg, sdp, lane, kk, &cw)) {
+                    int j;
+                    float wd;
+                    while (dd3_colwalk_next(Lg, &cw, &j, &wd)) {
+                        const float cf = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
 #pragma unroll
-                for (int q = 0; q < kRB; q++) {
-                    DdZ3 z;
-                    dd3_zstart(lz.x, lz.y, lz.z, rp0[q], rp1[q], &z);
-                    float zw;
-                    int s;
-                    while (dd3_zstep(&z, lz.z, Dp, &zw, &s)) {
-                        const float *__restrict__ ps = lsrc + (size_t)s * plane;
-#pragma unroll
-                        for (int t = 0; t < kNS; t++) {
-                            if (t < n) {
-                                const float wq = FMUL(zw, cs[t]);
+                        for (int q = 0; q < kFR; q++) {
+                            const float bz0 = fmaxf(lz.x, rp0[q]), bz1 = fminf(lz.y, rp1[q]);
+                            if (!(bz0 < bz1)) continue;
+                            for (int s = dd3_slice_first(bz0, lz.x, lz.z); s < Dp; s++) {
+                                const float zlo = dd3_zb(lz.x, lz.z, s);
+                                if (!(zlo < bz1)) break;
+                                const float zw = dd3_cell(bz0, bz1, zlo, dd3_zb(lz.x, lz.z, s + 1));
+                                if (!(zw > 0.0f)) continue;
+                                const float wq = FMUL(zw, cf);
+                                const float *__restrict__ ps = lsrc + (size_t)s * plane + j;
 #pragma unroll
                                 for (int b = 0; b < kNB; b++)
-                                    if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride + js[t]), acc[q][b]);
+                                    if (b < nb) acc[q][b] = fmaf(wq, __ldg(ps + (size_t)b * vstride), acc[q][b]);
                             }
                         }
                     }
                 }
             }
         }
-        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
+        __syncthreads();
+        // the record of line + 1 has been turned into segments: its buffer takes line + 3
+        if (tid == 0 && !abort_flag && line + 3 < nline) issue(line + 3, (line + 1) & 1);
     }
+    __syncthreads();
     if (abort_flag) {
-        // let a copy still in flight land before the CTA exits
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
-        if (tid == 0) atomicExch(a.status, DD_ERR_TIMEOUT);
+        // let copies still in flight land before the CTA exits
+        if (tid == 0) {
+            for (int b = 0; b < 2; b++)
+                if (nissue[b] > nwait[b]) dd_mbar_wait(&bar[b], (uint32_t)nwait[b] & 1u);
+            atomicExch(a.status, DD_ERR_TIMEOUT);
+        }
         return;
     }
     if (!active) return;
     const int ko = w.flip ? C - 1 - k : k;
 #pragma unroll
-    for (int q = 0; q < kRB; q++) {
+    for (int q = 0; q < kFR; q++) {
         const int r = r0 + q;
         if (r >= R) continue;
-        const float scale = (FAMILY == 0) ? dd3_proj_scale(&g, &w, sdp[kk], sdp[kk + 1], rp0[q], rp1[q]) : w.bp_scale;
+        const float scale = (FAMILY == 0) ? dd3_proj_scale(&g, &w, sdp[lane], sdp[lane + 1], rp0[q], rp1[q]) : w.bp_scale;
 #pragma unroll
         for (int b = 0; b < kNB; b++) {
             if (b < nb) {
@@ -546,7 +596,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
             const float4 lz = reinterpret_cast<const float4 *>(sm + S.lz + buf * S.lz_b)[rl];
             const DdLine *lrec = reinterpret_cast<const DdLine *>(sm + S.rec + buf * S.rec_b) + rl * P.nch;
             const float lpos = (FAMILY == 2) ? dd3_line_pos(&g, &w, line) : 0.0f;
-            const float margin = 0.25f * fabsf(lz.z);
+            float zb[kZS + 1];   // slice boundaries of the slab on this line
+#pragma unroll
+            for (int q = 0; q <= kZS; q++) zb[q] = dd3_zb(lz.x, lz.z, s0 + q);
             const float *__restrict__ ssv = ssb + (size_t)v * R * C;
             for (int cc = 0; cc < P.nch; cc++) {
                 DdPixWalk pw;
@@ -557,24 +609,39 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
                     const float coef = dd3_coef(GEOM, FAMILY, &g, &w, lpos, j, wd, lz.w);
                     const float mag = mg[k];
                     const float *__restrict__ ssk = ssv + k;
+                    // rows meeting each slice of the slab; the first row of
+                    // slice q + 1 is found from where slice q stopped
+                    int rnext = -1;
 #pragma unroll
                     for (int q = 0; q < kZS; q++) {
                         const int s = s0 + q;
                         if (s < Dp) {
-                            const float zlo = FADD(lz.x, FMUL((float)s, lz.z));
-                            const float zhi = FADD(zlo, lz.z);
-                            for (int r = dd3_row_first(GEOM, &w, rz, R, mag, zlo, margin); r < R; r++) {
+                            const float zlo = zb[q], zhi = zb[q + 1];
+                            int r;
+                            if (rnext < 0) {
+                                r = dd3_row_first(GEOM, &w, rz, R, mag, zlo, 0.0f);
+                            } else {
+                                r = max(rnext - 1, 0);
+                                for (int it = 0; it < 64 && r > 0; it++) {
+                                    float e0, e1;
+                                    dd3_rp(GEOM, &w, mag, rz[2 * (r - 1)], rz[2 * (r - 1) + 1], &e0, &e1);
+                                    if (e1 > zlo) r--;
+                                    else break;
+                                }
+                            }
+                            for (; r < R; r++) {
                                 float e0, e1;
                                 dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &e0, &e1);
-                                if (e0 >= zhi + margin) break;
-                                const float zw = dd3_zweight(lz.x, lz.y, lz.z, e0, e1, s, Dp);
-                                if (zw != 0.0f) {
+                                if (!(e0 < zhi)) break;
+                                const float zw = dd3_cell(fmaxf(lz.x, e0), fminf(lz.y, e1), zlo, zhi);
+                                if (zw > 0.0f) {
                                     const float wq = FMUL(zw, coef);
 #pragma unroll
                                     for (int b = 0; b < kNB; b++)
                                         if (b < nb) acc[q][b] = fmaf(wq, __ldg(ssk + (size_t)b * per + (size_t)r * C), acc[q][b]);
                                 }
                             }
+                            rnext = r;
                         }
                     }
                 }
@@ -665,7 +732,8 @@ int plan(int scan, const dd_geom3d *g, const float *angles, const float *sp, int
 
 template <int GEOM>
 int launch_fwd(int family, const Fwd3Args &a, cudaStream_t st) {
-    const dim3 grid((unsigned)a.V, (unsigned)a.P.nch, (unsigned)(a.nrb * ((a.B + kNB - 1) / kNB)));
+    const dim3 grid((unsigned)a.V, (unsigned)((a.g.num_col + kFC - 1) / kFC),
+                    (unsigned)(a.nrb * ((a.B + kNB - 1) / kNB)));
     dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_FORWARD, st);
     if (family == 0) k_fwd3<GEOM, 0><<<grid, kThreads, 0, st>>>(a);
     else if (family == 1) k_fwd3<GEOM, 1><<<grid, kThreads, 0, st>>>(a);
@@ -733,7 +801,7 @@ int forward(int scan, int op, const dd_geom3d *g, const char *planb, const float
     a.sub = sub;
     a.B = B;
     a.V = V;
-    a.nrb = (g->num_row + kRB - 1) / kRB;
+    a.nrb = (g->num_row + kFR * kWarps3 - 1) / (kFR * kWarps3);
     const int fam = op_family(op), geom = geom_of(scan);
     if (geom == DD_GEOM3_CONE_FLAT) return launch_fwd<DD_GEOM3_CONE_FLAT>(fam, a, st);
     if (geom == DD_GEOM3_CONE_ARC) return launch_fwd<DD_GEOM3_CONE_ARC>(fam, a, st);

@@ -57,22 +57,6 @@ static_assert(sizeof(DdLine) % 16 == 0, "DdLine must be a multiple of 16 bytes")
 // plane), pintz (slice pitch there), parea (pixel area for the DD-BP family).
 // Stored as float4 {p0z, p1z, pintz, parea}.
 
-// floor of the correctly rounded quotient num / den, as the reference's
-// FP32 walk computes it.  On the device an approximate quotient settles
-// every case that is not within a few ulp of an integer (where the rounded
-// and the approximate quotient must have the same floor); the remaining
-// cases take the correctly rounded division.
-DD_HD int dd3_floor_div(float num, float den) {
-#if defined(__CUDA_ARCH__)
-    if (fabsf(den) < 1.0e30f) {
-        const float q = __fdividef(num, den);
-        const float n = rintf(q);
-        if (fabsf(q - n) > 1.0e-6f * fmaxf(1.0f, fabsf(q)) && fabsf(q) < 1.0e9f) return (int)floorf(q);
-    }
-#endif
-    return dd_ifloor(FDIV(num, den));
-}
-
 // Approximate quotient for estimates that are corrected afterwards.
 DD_HD float dd3_approx_div(float num, float den) {
 #if defined(__CUDA_ARCH__)
@@ -398,44 +382,29 @@ DD_HD int dd3_pixel_of(const DdLine *L, float u, int *p) {
 }
 
 // ---------------------------------------------------------------------------
-// z walk of one (line, column, row) cell: the slices it meets and their
-// widths (ConeFlatDisCUDA3d.cu:131-152)
+// Closed-form z cells.  The reference's z walk starts each (line, column, row)
+// cell at bz0 = max(p0z, rp0) in slice is0 = floor((bz0 - p0z) / pintz), takes
+// is0 * pintz + p0z + pintz as the first slice top and then adds pintz once per
+// further slice (1-3 slices, so FP32 drift stays at the ulp level;
+// ConeFlatDisCUDA3d.cu:131-152).  Here the top of slice s is always
+// dd3_zb(s + 1) -- the reference's own formula for the first top -- and the
+// width of (row, slice) is the overlap of the row interval [bz0, bz1] with
+// [dd3_zb(s), dd3_zb(s + 1)].  Forward and adjoint evaluate the same
+// expression, so they stay exact transposes.
 // ---------------------------------------------------------------------------
-struct DdZ3 {
-    float bz0, bz1, pz1;
-    int is;
-};
+DD_HD float dd3_zb(float p0z, float pintz, int s) { return FADD(FMUL((float)s, pintz), p0z); }
 
-DD_HD void dd3_zstart(float p0z, float p1z, float pintz, float rp0, float rp1, DdZ3 *z) {
-    z->bz0 = p0z > rp0 ? p0z : rp0;
-    z->bz1 = p1z < rp1 ? p1z : rp1;
-    z->is = (z->bz0 == p0z) ? 0 : dd3_floor_div(FSUB(z->bz0, p0z), pintz);
-    z->pz1 = FADD(FMUL((float)(z->is + 1), pintz), p0z);
+DD_HD float dd3_cell(float bz0, float bz1, float zlo, float zhi) {
+    const float lo = bz0 > zlo ? bz0 : zlo;
+    const float hi = bz1 < zhi ? bz1 : zhi;
+    return hi > lo ? FSUB(hi, lo) : 0.0f;
 }
 
-// Width of the slice z->is and advance; false when the walk has ended.
-DD_HD bool dd3_zstep(DdZ3 *z, float pintz, int Dp, float *zw, int *slice) {
-    if (!(z->bz0 < z->bz1) || z->is >= Dp || z->is < 0) return false;
-    const float c = z->pz1 > z->bz1 ? z->bz1 : z->pz1;
-    *zw = FSUB(c, z->bz0);
-    *slice = z->is;
-    z->bz0 = c;
-    z->is++;
-    z->pz1 = FADD(c, pintz);
-    return true;
-}
-
-// Width of slice s in the walk of one cell (0 if the walk does not reach it).
-DD_HD float dd3_zweight(float p0z, float p1z, float pintz, float rp0, float rp1, int s, int Dp) {
-    DdZ3 z;
-    dd3_zstart(p0z, p1z, pintz, rp0, rp1, &z);
-    if (s < z.is) return 0.0f;
-    float zw = 0.0f;
-    int sl = -1;
-    while (dd3_zstep(&z, pintz, Dp, &zw, &sl)) {
-        if (sl == s) return zw;
-    }
-    return 0.0f;
+// First slice a row interval starting at bz0 can meet (one below the
+// estimate, so that no slice with a positive width is skipped).
+DD_HD int dd3_slice_first(float bz0, float p0z, float pintz) {
+    int s = (int)floorf(dd3_approx_div(FSUB(bz0, p0z), pintz)) - 1;
+    return s < 0 ? 0 : s;
 }
 
 // ---------------------------------------------------------------------------

@@ -95,9 +95,8 @@ extern "C" int model_apply3d(int geom, int op, const dd_geom3d *g, const float *
                         float acc = 0.0f;
                         for (int l = 0; l < nline; l++) {
                             const float *lz = &P.linez[((size_t)v * P.nl + l) * 4];
-                            DdZ3 z0;
-                            dd3_zstart(lz[0], lz[1], lz[2], rp0, rp1, &z0);
-                            if (!(z0.bz0 < z0.bz1)) continue;
+                            const float bz0 = lz[0] > rp0 ? lz[0] : rp0, bz1 = lz[1] < rp1 ? lz[1] : rp1;
+                            if (!(bz0 < bz1)) continue;
                             const DdLine &L = P.lines[((size_t)v * P.nl + l) * P.nch + cc];
                             DdColWalk cw;
                             if (!dd3_colwalk_init(&L, dp, k, kk, &cw)) continue;
@@ -106,11 +105,13 @@ extern "C" int model_apply3d(int geom, int op, const dd_geom3d *g, const float *
                             float wd;
                             while (dd3_colwalk_next(&L, &cw, &j, &wd)) {
                                 const float coef = dd3_coef(geom, family, g, &w, lpos, j, wd, lz[3]);
-                                DdZ3 z = z0;
-                                float zw;
-                                int s;
-                                while (dd3_zstep(&z, lz[2], Dp, &zw, &s))
-                                    acc = std::fmaf(FMUL(zw, coef), in[b * vox_b + vox_index(g, w, s, l, j)], acc);
+                                for (int s = dd3_slice_first(bz0, lz[0], lz[2]); s < Dp; s++) {
+                                    const float zlo = dd3_zb(lz[0], lz[2], s);
+                                    if (!(zlo < bz1)) break;
+                                    const float zw = dd3_cell(bz0, bz1, zlo, dd3_zb(lz[0], lz[2], s + 1));
+                                    if (zw > 0.0f)
+                                        acc = std::fmaf(FMUL(zw, coef), in[b * vox_b + vox_index(g, w, s, l, j)], acc);
+                                }
                             }
                         }
                         const float scale = (family == 0) ? dd3_proj_scale(g, &w, dp[k], dp[k + 1], rp0, rp1) : w.bp_scale;
@@ -152,8 +153,7 @@ extern "C" int model_apply3d(int geom, int op, const dd_geom3d *g, const float *
                         const int j = w.xb ? x : H - 1 - y;
                         const float *lz = &P.linez[((size_t)v * P.nl + line) * 4];
                         const float lpos = dd3_line_pos(g, &w, line);
-                        const float zlo = lz[0] + (float)s * lz[2], zhi = zlo + lz[2];
-                        const float margin = 0.25f * fabsf(lz[2]);
+                        const float zlo = dd3_zb(lz[0], lz[2], s), zhi = dd3_zb(lz[0], lz[2], s + 1);
                         for (int cc = 0; cc < P.nch; cc++) {
                             const DdLine &L = P.lines[((size_t)v * P.nl + line) * P.nch + cc];
                             DdPixWalk pw;
@@ -163,12 +163,13 @@ extern "C" int model_apply3d(int geom, int op, const dd_geom3d *g, const float *
                             while (dd3_pixwalk_next(dp, &pw, &k, &wd)) {
                                 const float coef = dd3_coef(geom, family, g, &w, lpos, j, wd, lz[3]);
                                 const float mag = P.mag[(size_t)v * C + k];
-                                for (int r = dd3_row_first(geom, &w, rz, R, mag, zlo, margin); r < R; r++) {
+                                for (int r = dd3_row_first(geom, &w, rz, R, mag, zlo, 0.0f); r < R; r++) {
                                     float rp0, rp1;
                                     dd3_rp(geom, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0, &rp1);
-                                    if (rp0 >= zhi + margin) break;
-                                    const float zw = dd3_zweight(lz[0], lz[1], lz[2], rp0, rp1, s, Dp);
-                                    if (zw != 0.0f)
+                                    if (!(rp0 < zhi)) break;
+                                    const float bz0 = lz[0] > rp0 ? lz[0] : rp0, bz1 = lz[1] < rp1 ? lz[1] : rp1;
+                                    const float zw = dd3_cell(bz0, bz1, zlo, zhi);
+                                    if (zw > 0.0f)
                                         acc = std::fmaf(FMUL(zw, coef), ss[b * det_b + ((size_t)v * R + r) * C + k], acc);
                                 }
                             }
