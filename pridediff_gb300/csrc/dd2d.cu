@@ -192,14 +192,51 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
+// Adjoint map of fan beams (plan time): for every (view, walked line,
+// boundary index b = -1 .. npix-1) the detector bin k and offset u - d_k of
+// the clamped boundary value u, exactly as the pixel-gather adjoint needs
+// them (k = -1 outside the walk), and the line's DD-BP scale.  Boundary
+// i0 - 1 is the walk start.  One thread per entry.
+template <int GEOM>
+__global__ void __launch_bounds__(128)
+k_amap(dd_geom2d g, int V, int nl, const DdView2 *__restrict__ views, const float *__restrict__ angles,
+       const float *__restrict__ dp, const DdLine *__restrict__ lines, int2 *__restrict__ amap,
+       float *__restrict__ alpha) {
+    const int e = blockIdx.x * 128 + threadIdx.x, line = blockIdx.y, v = blockIdx.z;
+    const int ms = map_stride(&g), D = g.num_det;
+    if (e >= ms) return;
+    const DdView2 vw = views[v];
+    const int nline = vw.xb ? g.height : g.width;
+    int2 *out = amap + ((size_t)v * nl + line) * ms + e;
+    if (line >= nline) {
+        *out = make_int2(-1, 0);
+        if (e == 0) alpha[(size_t)v * alpha_stride(nl) + line] = 0.0f;
+        return;
+    }
+    const DdLine &L = lines[(size_t)v * nl + line];
+    if (e == 0) alpha[(size_t)v * alpha_stride(nl) + line] = L.h.alpha;
+    const int b = e - 1, i0 = L.h.i0, nend = L.h.nend;
+    if (L.h.npiece == 0 || b < i0 - 1 || b >= nend) {
+        *out = make_int2(-1, 0);
+        return;
+    }
+    const float bound0 = L.h.bound0;
+    const float *dpv = dp + (size_t)v * (D + 1);
+    const float u = (b == i0 - 1) ? bound0 : dd_boundary(&L, b, L.p[0].Q + (float)(b - L.p[0].gb) * L.p[0].dl);
+    const float uu = fminf(fmaxf(u, bound0), dpv[D]);
+    float dk;
+    const int k = fan_bin(GEOM, g, vw, angles[v], dpv, uu, L.h.idet0, &dk);
+    *out = make_int2(k, __float_as_int(uu - dk));
+}
+
 // Single-geometry adjoint launch: grid (tiles x, tiles y, image groups).
 template <int GEOM, int OPK>
 __global__ void __launch_bounds__(kThreads)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const DdView2 *__restrict__ views, const float *__restrict__ dp,
-      const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines,
-      const float2 *__restrict__ dtab, float *__restrict__ out, const float *__restrict__ base,
-      float scale, int *__restrict__ status) {
+      const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines, const int2 *__restrict__ amap,
+      const float *__restrict__ alpha, const float2 *__restrict__ dtab, float *__restrict__ out,
+      const float *__restrict__ base, float scale, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
     init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar));
@@ -216,11 +253,16 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     it.dp = dp;
     it.lines = lines;
     it.dlines = dlines;
+    it.amap = amap;
+    it.alpha = alpha;
     it.dtab = dtab;
     it.out = out;
     it.base = base;
     it.scale = scale;
-    if (!adj_tile<GEOM, OPK>(g, it, smem, uses) && threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+    bool ok;
+    if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(g, it, smem, uses);
+    else ok = adj_tile_map<GEOM, OPK>(g, it, smem, uses);
+    if (!ok && threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
 }
 
 // ---------------------------------------------------------------------------
@@ -288,8 +330,8 @@ void prof_end(ProfRec *r, cudaStream_t st) {
 void count_launches(int n) { g_launches += (unsigned long long)n; }
 
 int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, size_t bytes,
-         cudaStream_t st) {
-    const PlanLayout P = plan_layout(scan, g, V);
+         cudaStream_t st, bool with_map) {
+    const PlanLayout P = plan_layout(scan, g, V, with_map);
     if (!planp || bytes < P.total) return DD_ERR_WORKSPACE;
     if (!angles) return DD_ERR_INVALID_ARG;
     char *base = (char *)planp;
@@ -303,8 +345,18 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
     k_views<<<V, 256, 0, st>>>(geom, *g, angles, V, views, (float *)(base + P.ang), dp, bc);
     dim3 gl((P.nl + 63) / 64, V);
     k_lines<<<gl, 64, 0, st>>>(geom, *g, angles, V, P.nl, views, dp, lines, dlines);
+    int n = 2;
+    if (geom != DD_GEOM_PARA && with_map) {
+        const dim3 gm((unsigned)((map_stride(g) + 127) / 128), (unsigned)P.nl, (unsigned)V);
+        const float *ang = (const float *)(base + P.ang);
+        int2 *amap = (int2 *)(base + P.amap);
+        float *alpha = (float *)(base + P.alpha);
+        if (geom == DD_GEOM_FLAT) k_amap<DD_GEOM_FLAT><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+        else k_amap<DD_GEOM_ARC><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+        n++;
+    }
     prof_end(pr, st);
-    g_launches += 2;
+    g_launches += n;
     return launch_status();
 }
 
@@ -348,13 +400,15 @@ static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const float *dp = (const float *)(planb + P.dp);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
+    const int2 *amap = GEOM == DD_GEOM_PARA ? nullptr : (const int2 *)(planb + P.amap);
+    const float *alpha = GEOM == DD_GEOM_PARA ? nullptr : (const float *)(planb + P.alpha);
     const AdjSmem S = adj_smem(GEOM);
     auto kern = (op == DD_OP_PROJ_T) ? k_adj<GEOM, 0> : (op == DD_OP_BPROJ) ? k_adj<GEOM, 1> : k_adj<GEOM, 2>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
-    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, dtab, out, base,
-                                          scale, status);
+    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, amap, alpha, dtab, out,
+                                          base, scale, status);
     prof_end(pr, st);
     g_launches++;
     return launch_status();
@@ -444,7 +498,7 @@ extern "C" size_t dd2d_apply_workspace_bytes(int scan, int op, const dd_geom2d *
 
 extern "C" size_t dd2d_workspace_bytes(int scan, int op, const dd_geom2d *g, int batch, int num_view) {
     if (!g || batch <= 0 || num_view <= 0) return 0;
-    return plan_layout(scan, g, num_view).total + apply_layout(op, g, batch, num_view).total;
+    return plan_layout(scan, g, num_view, !op_is_forward(op)).total + apply_layout(op, g, batch, num_view).total;
 }
 
 extern "C" int dd2d_plan(int scan, const dd_geom2d *g, const float *angles, int num_view, void *planp,
@@ -460,10 +514,12 @@ extern "C" int dd2d_apply(int scan, int op, const dd_geom2d *g, const float *in,
     const int st = validate(scan, op, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!angles || !in || !out) return DD_ERR_INVALID_ARG;
-    const size_t pb = plan_layout(scan, g, num_view).total;
+    // a one-shot forward-type call needs no adjoint map in its plan
+    const bool with_map = !op_is_forward(op);
+    const size_t pb = plan_layout(scan, g, num_view, with_map).total;
     if (!workspace || workspace_bytes < dd2d_workspace_bytes(scan, op, g, batch, num_view))
         return DD_ERR_WORKSPACE;
-    const int s1 = plan(scan, g, angles, num_view, workspace, pb, (cudaStream_t)stream);
+    const int s1 = plan(scan, g, angles, num_view, workspace, pb, (cudaStream_t)stream, with_map);
     if (s1 != DD_OK) return s1;
     return apply_planned(scan, op, g, workspace, in, out, batch, num_view, (char *)workspace + pb,
                          workspace_bytes - pb, (cudaStream_t)stream);

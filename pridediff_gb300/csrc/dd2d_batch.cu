@@ -33,7 +33,7 @@ struct BatchInst {
     long long img_off, sino_off;   // elements: packed images / sinograms
     long long tabx_off, taby_off;  // float2: forward tables in the workspace
     long long dtab_off;            // float2: adjoint tables in the workspace
-    long long views, ang, dp, bcoef, lines, dlines;   // PlanLayout offsets
+    long long views, ang, dp, bcoef, lines, dlines, amap, alpha;   // PlanLayout offsets
 };
 
 struct BatchLayout {
@@ -67,6 +67,8 @@ static BatchLayout batch_layout(int scan, const dd_instance2d *in, int n, int bi
         d.bcoef = (long long)P.bcoef;
         d.lines = (long long)P.lines;
         d.dlines = (long long)P.dlines;
+        d.amap = (long long)P.amap;
+        d.alpha = (long long)P.alpha;
         const int W = d.g.width, H = d.g.height, D = d.g.num_det;
         d.img_off = img;
         img += (long long)d.batch * H * W;
@@ -264,11 +266,16 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
         it.dp = reinterpret_cast<const float *>(pb + d.dp);
         it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
         it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
+        it.amap = reinterpret_cast<const int2 *>(pb + d.amap);
+        it.alpha = reinterpret_cast<const float *>(pb + d.alpha);
         it.dtab = dtabs + d.dtab_off;
         it.out = out + d.img_off;
         it.base = base ? base + d.img_off : nullptr;
         it.scale = scale;
-        if (!adj_tile<GEOM, OPK>(d.g, it, smem, uses)) {
+        bool ok;
+        if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(d.g, it, smem, uses);
+        else ok = adj_tile_map<GEOM, OPK>(d.g, it, smem, uses);
+        if (!ok) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }

@@ -26,11 +26,22 @@ __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n
 // Workspace layout
 // ---------------------------------------------------------------------------
 struct PlanLayout {
-    size_t views, ang, dp, bcoef, lines, dlines, total;
+    size_t views, ang, dp, bcoef, lines, dlines, amap, alpha, total;
     int nl;   // line records per view = max(H, W)
 };
 
-inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V) {
+// Adjoint map of fan beams: per (view, walked line) a row of map_stride()
+// entries {bin k, offset} for the boundary indices -1 .. npix-1 (entry e holds
+// boundary e - 1); alpha_stride() per-line DD-BP scales per view.
+__host__ __device__ inline int map_stride(const dd_geom2d *g) {
+    return rs_entries(g->width > g->height ? g->width : g->height);
+}
+__host__ __device__ inline int alpha_stride(int nl) { return (nl + 31) & ~31; }
+
+// with_map = false leaves out the adjoint map (plans that only serve the
+// forward-type operators, e.g. one-shot forward calls); every other offset is
+// the same either way.
+inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V, bool with_map = true) {
     PlanLayout L;
     const int D = g->num_det;
     L.nl = g->height > g->width ? g->height : g->width;
@@ -42,6 +53,11 @@ inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V) {
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
     L.dlines = o;
     if (scan == DD_SCAN_PARA) o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
+    L.amap = L.alpha = o;
+    if (scan != DD_SCAN_PARA && with_map) {
+        L.amap = o; o = align_up(o + sizeof(int2) * (size_t)V * L.nl * map_stride(g), 256);
+        L.alpha = o; o = align_up(o + sizeof(float) * (size_t)V * alpha_stride(L.nl), 256);
+    }
     L.total = o;
     return L;
 }
@@ -398,14 +414,32 @@ __device__ __forceinline__ void det_index_fan(int geom, const dd_geom2d &g, cons
 // gather from global memory instead.
 constexpr int kStage = 256;
 
-// Shared-memory layout of the adjoint kernel (bytes).
+// Staged adjoint-map entries per line and view: the boundaries of a 32-pixel
+// run plus one below it, from an even first entry.
+constexpr int kMapE = 36;
+
+// Shared-memory layout of the adjoint kernel (bytes).  Parallel beam: line
+// records (and detector-side records); fan beams: adjoint-map rows, detector
+// table slices and per-line scales.
 struct AdjSmem {
     int rec, drec, kd, stage, krange, bar, total;
+    int map, alpha;
 };
 
 __host__ __device__ inline AdjSmem adj_smem(int geom) {
     AdjSmem s;
     int o = 0;
+    s.map = s.alpha = 0;
+    if (geom != DD_GEOM_PARA) {
+        s.rec = s.drec = s.kd = 0;
+        s.map = o; o += 2 * kTile * kMapE * (int)sizeof(int2);
+        s.stage = o; o += 2 * kBI * kStage * (int)sizeof(float2);
+        s.alpha = o; o += 2 * kTile * (int)sizeof(float);
+        s.krange = o; o += 8 * (int)sizeof(int);
+        s.bar = o; o += 2 * (int)sizeof(uint64_t);
+        s.total = (o + 127) & ~127;
+        return s;
+    }
     s.rec = o; o += 2 * kTile * (int)sizeof(DdLine);
     s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * kTile * (int)sizeof(DdLine);
     s.kd = o; if (geom == DD_GEOM_PARA) o += kWarps * kBI * 32 * (int)sizeof(float);
@@ -477,6 +511,8 @@ struct AdjItem {
     const DdView2 *views;
     const float *dp;
     const DdLine *lines, *dlines;
+    const int2 *amap;            // fan beams: adjoint map (plan)
+    const float *alpha;          // fan beams: per-line DD-BP scales (plan)
     const float2 *dtab;          // detector tables of image 0 of the instance
     float *out;                  // image 0 of the instance
     const float *base;
@@ -718,13 +754,165 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
 }
 
 
+// ---------------------------------------------------------------------------
+// Fan-beam adjoint through the adjoint map.  For every view the CTA copies by
+// TMA, for its 32 walked lines, the map entries {bin, offset} of the tile's
+// pixel boundaries, the per-line scales and the slice of every image's
+// detector prefix table the tile can reach.  A thread owns fixed pixels (warp
+// = rows, lane = column) for every view, so one set of accumulators serves
+// both projection axes: pixel value += w (H(upper) - H(lower)), with
+// H(u) = G_k + (u - d_k) g_k read at the two staged boundary entries.
+// ---------------------------------------------------------------------------
+template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
+__device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, uint32_t *uses) {
+    const AdjSmem SL = adj_smem(GEOM);
+    const int V = it.V, nl = it.nl;
+    const int W = g.width, H = g.height, D = g.num_det;
+    const int rsd = rs_entries(D), ms = map_stride(&g), sal = alpha_stride(nl);
+    int2 *mapb = reinterpret_cast<int2 *>(smem + SL.map);          // [2][kTile][kMapE]
+    float2 *stage = reinterpret_cast<float2 *>(smem + SL.stage);   // [2][kBI][kStage]
+    float *alb = reinterpret_cast<float *>(smem + SL.alpha);       // [2][kTile]
+    int *krange = reinterpret_cast<int *>(smem + SL.krange);       // per buffer: first bin, bins, first entry
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SL.bar);
+    __shared__ int abort_flag;
+    const int c0 = it.c0, r0 = it.r0, b0 = it.b0, nb = it.nb;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float2 *__restrict__ dtab = it.dtab;
+    if (tid == 0) abort_flag = 0;
+    __syncthreads();
+
+    // warp 0: copies of view v into buffer buf (lane i moves line i's entries)
+    auto issue = [&](int v, int buf) {
+        const DdView2 vwv = it.views[v];
+        const int xbv = vwv.xb;
+        const int l0 = xbv ? r0 : c0;
+        const int nlines = min(kTile, (xbv ? H : W) - l0);
+        int elo, ne;
+        if (xbv) {   // pixels c0 .. c0+31 of rows r0 ..: boundaries c0-1 .. c0+31
+            elo = c0;
+            ne = min(kTile + 2, ms - c0);
+        } else {     // pixels H-r0-32 .. H-r0-1 of columns c0 ..
+            const int lo = max(H - r0 - kTile, 0) & ~1;
+            const int hi = min(H - r0 + 1, ms);
+            elo = lo;
+            ne = (hi - lo + 1) & ~1;
+        }
+        int kmin, kmax;
+        tile_bin_range(GEOM, g, vwv, it.angles[v], c0, r0, &kmin, &kmax);
+        const int kb = kmin & ~1;
+        int kn = (kmax - kb + 2) & ~1;
+        if (kb + kn > rsd) kn = rsd - kb;
+        if (kn > kStage || kn <= 0) kn = 0;
+        if (lane == 0) {
+            krange[4 * buf] = kb;
+            krange[4 * buf + 1] = kn;
+            krange[4 * buf + 2] = elo;
+            dd_mbar_expect_tx(&bar[buf], (uint32_t)((nlines * ne + nb * kn) * (int)sizeof(int2) + kTile * (int)sizeof(float)));
+        }
+        __syncwarp();
+        if (lane < nlines)
+            dd_bulk_g2s(mapb + ((size_t)buf * kTile + lane) * kMapE, it.amap + ((size_t)v * nl + l0 + lane) * ms + elo,
+                        (uint32_t)(ne * sizeof(int2)), &bar[buf]);
+        if (lane < nb && kn > 0)
+            dd_bulk_g2s(stage + ((size_t)buf * kBI + lane) * kStage, dtab + ((size_t)(b0 + lane) * V + v) * rsd + kb,
+                        (uint32_t)(kn * sizeof(float2)), &bar[buf]);
+        if (lane == 31)
+            dd_bulk_g2s(alb + buf * kTile, it.alpha + (size_t)v * sal + l0, (uint32_t)(kTile * sizeof(float)), &bar[buf]);
+    };
+
+    float acc[kLinesPerWarp][kBI];
+#pragma unroll
+    for (int q = 0; q < kLinesPerWarp; q++)
+#pragma unroll
+        for (int b = 0; b < kBI; b++) acc[q][b] = 0.0f;
+
+    if (warp == 0) issue(0, 0);
+    int inflight = -1;
+    for (int v = 0; v < V; v++) {
+        const int buf = v & 1;
+        if (warp == 0 && v + 1 < V) issue(v + 1, buf ^ 1);
+        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
+        uses[buf]++;
+        __syncthreads();
+        if (abort_flag) {
+            inflight = (v + 1 < V) ? (buf ^ 1) : -1;
+            break;
+        }
+        const DdView2 vw = it.views[v];
+        const int xb = vw.xb;
+        const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
+        const int2 *mp = mapb + (size_t)buf * kTile * kMapE;
+        const float2 *sb = stage + (size_t)buf * kBI * kStage;
+#pragma unroll
+        for (int q = 0; q < kLinesPerWarp; q++) {
+            const int r = r0 + warp + kWarps * q, c = c0 + lane;
+            if (r >= H || c >= W) continue;
+            int lr, eu;
+            if (xb) {
+                lr = r - r0;
+                eu = c + 1 - elo;
+            } else {
+                lr = c - c0;
+                eu = H - r - elo;
+            }
+            const int2 up = mp[lr * kMapE + eu], low = mp[lr * kMapE + eu - 1];
+            if (up.x < 0 || low.x < 0) continue;
+            float wgt = (OPK == 0) ? 1.0f : alb[buf * kTile + lr];
+            if (OPK == 2) {
+                const int line = xb ? r : c, pi = xb ? c : H - 1 - r;
+                float pcx, pcy;
+                if (xb) {
+                    pcx = (float)(((double)pi + 0.5) * (double)g.pix_x + (double)vw.axis0);
+                    pcy = (float)(((double)H / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift);
+                } else {
+                    pcx = (float)(((double)line - W / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
+                    pcy = (float)(((double)pi + 0.5) * (double)g.pix_y + (double)vw.axis0);
+                }
+                wgt = wgt * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
+                                                   : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
+            }
+            const float offU = __int_as_float(up.y), offL = __int_as_float(low.y);
+            const bool inU = (unsigned)(up.x - kb) < (unsigned)kn;
+            const bool inL = (unsigned)(low.x - kb) < (unsigned)kn;
+#pragma unroll
+            for (int b = 0; b < kBI; b++) {
+                if (b >= nb) break;
+                const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
+                const float2 e = inU ? sb[b * kStage + (up.x - kb)] : __ldg(t + up.x);
+                const float2 e2 = inL ? sb[b * kStage + (low.x - kb)] : __ldg(t + low.x);
+                const float hu = fmaf(offU, e.y, e.x);
+                const float hl = fmaf(offL, e2.y, e2.x);
+                acc[q][b] += wgt * (hu - hl);
+            }
+        }
+        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
+    }
+    if (abort_flag) {
+        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
+        if (inflight >= 0) uses[inflight]++;
+        __syncthreads();
+        return false;
+    }
+#pragma unroll
+    for (int q = 0; q < kLinesPerWarp; q++) {
+        const int r = r0 + warp + kWarps * q, c = c0 + lane;
+        if (r >= H || c >= W) continue;
+        for (int b = 0; b < nb; b++) {
+            const size_t o = ((size_t)(b0 + b) * H + r) * W + c;
+            it.out[o] = it.base ? fmaf(it.scale, acc[q][b], it.base[o]) : acc[q][b];
+        }
+    }
+    return true;
+}
+
+
 // ---- host launchers shared by both translation units (dd2d.cu) -----------
 struct ProfRec;
 ProfRec *prof_begin(int kind, cudaStream_t st);
 void prof_end(ProfRec *r, cudaStream_t st);
 void count_launches(int n);
 int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, size_t bytes,
-         cudaStream_t st);
+         cudaStream_t st, bool with_map = true);
 int validate(int scan, int op, const dd_geom2d *g, int B, int V);
 int geom_of(int scan);
 int launch_status();

@@ -80,8 +80,13 @@ def test_apply_rejects_missing_workspace_and_pointers(lib):
     fake = ctypes.c_void_p(0x1000)
     assert lib.dd2d_apply(1, 0, g, fake, fake, fake, 1, 10, None, 0, None) == N.DD_ERR_WORKSPACE
     assert lib.dd2d_apply(1, 0, g, fake, fake, fake, 1, 10, fake, 16, None) == N.DD_ERR_WORKSPACE
-    need = lib.dd2d_workspace_bytes(1, 0, g, 1, 10)
-    assert need > lib.dd2d_plan_bytes(1, g, 10) > 0
+    # a one-shot adjoint carries the full plan (with the adjoint map); a
+    # one-shot forward leaves the map out and needs less than a reusable plan
+    need_adj = lib.dd2d_workspace_bytes(1, 1, g, 1, 10)
+    assert need_adj > lib.dd2d_plan_bytes(1, g, 10) > 0
+    need_fwd = lib.dd2d_workspace_bytes(1, 0, g, 1, 10)
+    assert 0 < need_fwd < need_adj
+    assert lib.dd2d_apply(1, 0, g, fake, fake, fake, 1, 10, fake, need_fwd - 1, None) == N.DD_ERR_WORKSPACE
     assert lib.dd2d_plan(1, g, None, 10, fake, 1 << 30, None) == N.DD_ERR_INVALID_ARG
 
 
