@@ -11,7 +11,13 @@ adjoint A^T r for every slice, through projector2d and its autograd pair.
 
 Metric: FP+BP per second (slice forward + adjoint pairs per second).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
+
+On one GPU the line also carries `extra`: the same slices through the plain
+per-slice path (the unbatched comparator), the 24-instance uneven batched
+data-consistency loop captured in a CUDA graph, and the 3-D cone-flat and
+spiral configurations, each with its view-swept bytes against the measured
+HBM peak.
 
 --impl reference times deeprecon's CPU algorithm on this host (the oracle
 port of it; the reference sources are not present here) on the same
@@ -189,6 +195,176 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _ellipsoids(shape, n, seed, scale, dev):
+    """Sum of n seeded random ellipsoids (intensity U[0, 1]) on the device."""
+    import torch
+    g = np.random.default_rng(seed)
+    D, H, W = shape
+    z = torch.arange(D, device=dev, dtype=torch.float32)[:, None, None]
+    y = torch.arange(H, device=dev, dtype=torch.float32)[None, :, None]
+    x = torch.arange(W, device=dev, dtype=torch.float32)[None, None, :]
+    vol = torch.zeros(shape, device=dev)
+    for _ in range(n):
+        c = [g.uniform(0.2, 0.8) * s for s in (D, H, W)]
+        a = [g.uniform(0.05, 0.3) * s for s in (D, H, W)]
+        inside = ((z - c[0]) / a[0]) ** 2 + ((y - c[1]) / a[1]) ** 2 + ((x - c[2]) / a[2]) ** 2 <= 1
+        vol += inside.float() * float(g.uniform(0, 1))
+    return vol * scale
+
+
+def _timed(fn, reps, flush, ev):
+    """Mean ms of fn over reps, CUDA events on the current stream, L2 flushed before each."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    tot = 0.0
+    for i in range(reps):
+        flush.fill_(float(i))
+        a, b = ev(), ev()
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        tot += a.elapsed_time(b)
+    return tot / reps
+
+
+def run_extras(dev, flush, peak, step2d, x0, y, B):
+    """The other configurations of this path, each timed on its own (one GPU)."""
+    import torch
+    import pridediff_gb300 as P
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+    out = {}
+
+    def frac(bytes_, ms):
+        gbs = bytes_ / (ms / 1e3) / 1e9
+        return {"achieved_GBps": gbs, "frac_of_measured_peak": gbs / peak}
+
+    # plain single-instance GPU path: the same 16 slices one call at a time
+    try:
+        def plain():
+            for i in range(B):
+                step2d(x0[i:i + 1], y[i:i + 1])
+        ms = _timed(plain, 3, flush, ev)
+        out["plain_per_slice"] = {"what": "headline workload, one slice per autograd call (no batching, no graph)",
+                                  "ms_per_step": ms, "value": B / (ms / 1e3), "unit": UNIT}
+    except Exception as e:   # report, never hide the headline line
+        out["plain_per_slice"] = {"error": repr(e)}
+
+    # batched uneven DC loop: 24 instances, 50 graph-captured steps, eta 1e-3
+    try:
+        from pridediff_gb300.batch import UnevenBatch2d
+        from pridediff_gb300 import autotune
+        rng = np.random.default_rng(2024)
+        projs, angs, imgs, nbytes = [], [], [], 0.0
+        for _ in range(24):
+            n = int(rng.choice([256, 384, 512]))
+            V = int(rng.choice([360, 576, 720]))
+            D = int(rng.choice([368, 512, 736]))
+            projs.append(P.projector2d(n, D, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").to(dev))
+            angs.append(torch.arange(V, dtype=torch.float32, device=dev) * (2 * np.pi / V))
+            imgs.append(torch.from_numpy(phantom(n, n, 10, rng, 0.04))[None, None].to(dev))
+            nbytes += 2 * 4.0 * V * (n * n + D)
+        ub = UnevenBatch2d(projs, angs)
+        xt = ub.pack(imgs)
+        yb = ub.forward(xt)
+        xs = (xt * 0.8).contiguous()
+        import tempfile
+        tune = autotune.tune_batch_dc(ub, xs, yb, eta=0.0, reps=2,
+                                      path=os.path.join(tempfile.gettempdir(), "pridediff_bench_tune.json"))
+        steps = 50
+        xg = xs.clone()
+        graph = ub.dc_graph(xg, yb, 1e-3, steps)
+        ms = _timed(lambda: graph.replay(), 3, flush, ev)
+        xe = xs.clone()
+        ms_eager = _timed(lambda: ub.dc_step(xe, yb, 1e-3), 3, flush, ev)
+        out["batched_dc_24_uneven"] = {
+            "what": "24 uneven fan-flat instances (image {256,384,512}^2, views {360,576,720}, dets "
+                    "{368,512,736}), x <- x - 1e-3 A^T(Ax - y), 50 steps in one CUDA graph, one persistent "
+                    "launch per operator, launch shape autotuned",
+            "tune": tune, "ms_per_step": ms / steps, "ms_per_step_eager_no_graph": ms_eager,
+            "value": 24 * steps / (ms / 1e3), "unit": UNIT, **frac(nbytes, ms / steps),
+            "bytes_model": "view-swept 4*V*(H*W + D) per instance and operator, FP + BP per step"}
+        del ub, graph, xg, xe, xs, yb, xt
+    except Exception as e:
+        out["batched_dc_24_uneven"] = {"error": repr(e)}
+    torch.cuda.empty_cache()
+
+    # 3-D cone-flat: 2 x 256^3, 360 views, 512 x 384 detector, autograd FP + BP
+    try:
+        proj = P.projector3d((256, 256, 256), (512, 384), 1.0, 1.0, 500.0, 1000.0, scan_type="flat").to(dev)
+        ang = torch.arange(360, dtype=torch.float32, device=dev) * (2 * np.pi / 360)
+        x3 = torch.stack([_ellipsoids((256, 256, 256), 12, 40 + i, 1.0, dev) for i in range(2)])[:, None]
+        with torch.no_grad():
+            y3 = proj.projection(x3, ang)
+
+        def step3():
+            xr = x3.detach().requires_grad_(True)
+            ((proj.projection(xr, ang) - y3) ** 2).sum().backward()
+        ms = _timed(step3, 3, flush, ev)
+        nb3 = 2 * 2 * 4.0 * 360 * (256 ** 3 + 384 * 512)
+        out["cone_flat_2x256^3"] = {"what": "cone-flat 2 x 256^3, 360 views, 512 x 384 detector, loss + backward",
+                                    "ms_per_step": ms, "value": 2 / (ms / 1e3), "unit": UNIT, **frac(nb3, ms),
+                                    "bytes_model": "view-swept 4*V*(W*H*D + R*C) per volume and operator"}
+        del proj, x3, y3
+    except Exception as e:
+        out["cone_flat_2x256^3"] = {"error": repr(e)}
+    torch.cuda.empty_cache()
+
+    # 3-D spiral: 2 x 512x512x128, 3456 views, 64 x 736 arc detector, graph-captured DC steps
+    try:
+        import ctypes
+        from pridediff_gb300 import _native as N
+        from pridediff_gb300 import radontorch as RT
+        V = 3456
+        pitch = 1.0 * 64 * 1.0 * 595.0 / 1085.6 / 1152
+        sp = torch.zeros((4, V), device=dev)
+        sp[0] = -pitch * (V - 1) / 2 + pitch * torch.arange(V, device=dev, dtype=torch.float32)
+        projs = P.projectorsp((512, 512, 128), (736, 64), (0.66, 0.66, 1.0), (1.2858, 1.0), 595.0, 1085.6).to(dev)
+        ang = torch.arange(V, dtype=torch.float32, device=dev) * (2 * np.pi / 1152)
+        x5 = torch.stack([_ellipsoids((128, 512, 512), 12, 60 + i, 0.04, dev) for i in range(2)])
+        g5 = N.geom3d(RT.host_options(projs.options), spiral=True)
+        lib = N.load()
+        plan = RT.plan3d("spiral", g5, ang, sp)
+        with torch.no_grad():
+            y5 = projs.projection(x5[:, None], ang, sp)[:, 0].contiguous()
+        nws = int(lib.dd3d_dc_workspace_bytes(2, g5, 2, V))
+        ws = torch.empty(nws, dtype=torch.uint8, device=dev)
+        resid = torch.empty_like(y5)
+        xs5 = (x5 * 0.8).contiguous()
+        steps = 5
+
+        def dc():
+            st = lib.dd3d_dc_step(2, g5, plan.data_ptr(), xs5.data_ptr(), y5.data_ptr(), resid.data_ptr(),
+                                  ctypes.c_float(1e-3), 2, V, ws.data_ptr(), nws,
+                                  torch.cuda.current_stream(dev).cuda_stream)
+            if st != 0:
+                raise RuntimeError(N.status_string(st))
+        dc()
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(dev)
+        s.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(graph, stream=s):
+                for _ in range(steps):
+                    dc()
+        torch.cuda.current_stream(dev).wait_stream(s)
+        ms = _timed(lambda: graph.replay(), 1, flush, ev) / steps
+        zeff = 64 * 1.0 * 595.0 / 1085.6 / 1.0
+        nb5 = 2 * 2 * 4.0 * V * (512 * 512 * zeff + 64 * 736)
+        out["spiral_2x512x512x128"] = {
+            "what": "spiral 2 x 512x512x128 (0.66 x 0.66 x 1.0 mm), 3456 views (3 turns, pitch 1), 64 x 736 arc "
+                    "detector; DC steps x <- x - 1e-3 A^T(Ax - y), 5 steps in one CUDA graph (the configuration "
+                    "runs 20)", "ms_per_step": ms, "value": 2 / (ms / 1e3), "unit": UNIT, **frac(nb5, ms),
+            "bytes_model": "view-swept 4*V*(W*H*Z_eff + R*C), Z_eff = 35.08 slices, per volume and operator"}
+        del graph, plan, ws, x5, xs5, y5, resid
+    except Exception as e:
+        out["spiral_2x512x512x128"] = {"error": repr(e)}
+    torch.cuda.empty_cache()
+    return out
+
+
 def workload_config():
     return {"workload": "fan-flat DD FP + exact-adjoint BP with autograd, 16 x 512^2 slices, "
                         "720 views over 360 deg, 736 dets x 1.2858 mm, SID 595, SDD 1085.6",
@@ -204,6 +380,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other configurations (batched DC loop, plain per-slice calls, 3-D)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -320,6 +498,13 @@ def main():
         e2e_ms = float(t.item())
     e2e_value = world * B / (e2e_ms / 1e3)
 
+    extras = None
+    if world == 1 and not args.no_extras:
+        extras = run_extras(dev, flush, peak, step, x0, y, B)
+        plain = extras.get("plain_per_slice", {}).get("value")
+        if plain:
+            extras["batched_over_plain"] = value / plain
+
     if rank == 0:
         cpu = None if args.no_cpu_baseline else cpu_port_baseline()
         line = {
@@ -342,6 +527,8 @@ def main():
             "wall_s_timed_region": wall,
             "cpu_baseline": cpu,
         }
+        if extras is not None:
+            line["extra"] = extras
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
