@@ -229,13 +229,37 @@ k_amap(dd_geom2d g, int V, int nl, const DdView2 *__restrict__ views, const floa
     *out = make_int2(k, __float_as_int(uu - dk));
 }
 
+// Detector-table slice staged per (view, 32x32 tile) by the fan-beam adjoint
+// (plan time): the tile's bin range (tile_bin_range) rounded to an even first
+// bin and an even count (16-byte bulk copies), or count 0 when wider than the
+// staging buffer.  One thread per (view, tile).
+template <int GEOM>
+__global__ void __launch_bounds__(128)
+k_trange(dd_geom2d g, int V, const DdView2 *__restrict__ views, const float *__restrict__ angles,
+         int2 *__restrict__ trange) {
+    const int nt = tiles_n(&g);
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    if (i >= V * nt) return;
+    const int v = i / nt, t = i - v * nt;
+    const int c0 = (t % tiles_x(&g)) * kTile, r0 = (t / tiles_x(&g)) * kTile;
+    int kmin, kmax;
+    tile_bin_range(GEOM, g, views[v], angles[v], c0, r0, &kmin, &kmax);
+    const int rsd = rs_entries(g.num_det);
+    const int kb = kmin & ~1;
+    int kn = (kmax - kb + 2) & ~1;
+    if (kb + kn > rsd) kn = rsd - kb;
+    if (kn > kStage || kn <= 0) kn = 0;
+    trange[i] = make_int2(kb, kn);
+}
+
 // Single-geometry adjoint launch: grid (tiles x, tiles y, image groups).
 template <int GEOM, int OPK>
 __global__ void __launch_bounds__(kThreads)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const DdView2 *__restrict__ views, const float *__restrict__ dp,
       const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines, const int2 *__restrict__ amap,
-      const float *__restrict__ alpha, const float2 *__restrict__ dtab, float *__restrict__ out,
+      const float *__restrict__ alpha, const int2 *__restrict__ trange, const float2 *__restrict__ dtab,
+      float *__restrict__ out,
       const float *__restrict__ base, float scale, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
@@ -255,6 +279,7 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     it.dlines = dlines;
     it.amap = amap;
     it.alpha = alpha;
+    it.trange = trange;
     it.dtab = dtab;
     it.out = out;
     it.base = base;
@@ -351,9 +376,16 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
         const float *ang = (const float *)(base + P.ang);
         int2 *amap = (int2 *)(base + P.amap);
         float *alpha = (float *)(base + P.alpha);
-        if (geom == DD_GEOM_FLAT) k_amap<DD_GEOM_FLAT><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
-        else k_amap<DD_GEOM_ARC><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
-        n++;
+        int2 *trange = (int2 *)(base + P.trange);
+        const int nt = (V * tiles_n(g) + 127) / 128;
+        if (geom == DD_GEOM_FLAT) {
+            k_amap<DD_GEOM_FLAT><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+            k_trange<DD_GEOM_FLAT><<<nt, 128, 0, st>>>(*g, V, views, ang, trange);
+        } else {
+            k_amap<DD_GEOM_ARC><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+            k_trange<DD_GEOM_ARC><<<nt, 128, 0, st>>>(*g, V, views, ang, trange);
+        }
+        n += 2;
     }
     prof_end(pr, st);
     g_launches += n;
@@ -402,13 +434,14 @@ static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
     const int2 *amap = GEOM == DD_GEOM_PARA ? nullptr : (const int2 *)(planb + P.amap);
     const float *alpha = GEOM == DD_GEOM_PARA ? nullptr : (const float *)(planb + P.alpha);
+    const int2 *trange = GEOM == DD_GEOM_PARA ? nullptr : (const int2 *)(planb + P.trange);
     const AdjSmem S = adj_smem(GEOM);
     auto kern = (op == DD_OP_PROJ_T) ? k_adj<GEOM, 0> : (op == DD_OP_BPROJ) ? k_adj<GEOM, 1> : k_adj<GEOM, 2>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
-    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, amap, alpha, dtab, out,
-                                          base, scale, status);
+    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, amap, alpha, trange,
+                                          dtab, out, base, scale, status);
     prof_end(pr, st);
     g_launches++;
     return launch_status();

@@ -26,7 +26,7 @@ __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n
 // Workspace layout
 // ---------------------------------------------------------------------------
 struct PlanLayout {
-    size_t views, ang, dp, bcoef, lines, dlines, amap, alpha, total;
+    size_t views, ang, dp, bcoef, lines, dlines, amap, alpha, trange, total;
     int nl;   // line records per view = max(H, W)
 };
 
@@ -37,6 +37,9 @@ __host__ __device__ inline int map_stride(const dd_geom2d *g) {
     return rs_entries(g->width > g->height ? g->width : g->height);
 }
 __host__ __device__ inline int alpha_stride(int nl) { return (nl + 31) & ~31; }
+// 32 x 32 tiles of the image (the adjoint's work items); tile = ty * ntx + tx
+__host__ __device__ inline int tiles_x(const dd_geom2d *g) { return (g->width + 31) / 32; }
+__host__ __device__ inline int tiles_n(const dd_geom2d *g) { return tiles_x(g) * ((g->height + 31) / 32); }
 
 // with_map = false leaves out the adjoint map (plans that only serve the
 // forward-type operators, e.g. one-shot forward calls); every other offset is
@@ -53,10 +56,11 @@ inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V, bool with_map
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
     L.dlines = o;
     if (scan == DD_SCAN_PARA) o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
-    L.amap = L.alpha = o;
+    L.amap = L.alpha = L.trange = o;
     if (scan != DD_SCAN_PARA && with_map) {
         L.amap = o; o = align_up(o + sizeof(int2) * (size_t)V * L.nl * map_stride(g), 256);
         L.alpha = o; o = align_up(o + sizeof(float) * (size_t)V * alpha_stride(L.nl), 256);
+        L.trange = o; o = align_up(o + sizeof(int2) * (size_t)V * tiles_n(g), 256);
     }
     L.total = o;
     return L;
@@ -513,6 +517,7 @@ struct AdjItem {
     const DdLine *lines, *dlines;
     const int2 *amap;            // fan beams: adjoint map (plan)
     const float *alpha;          // fan beams: per-line DD-BP scales (plan)
+    const int2 *trange;          // fan beams: staged detector-table slice per (view, tile) (plan)
     const float2 *dtab;          // detector tables of image 0 of the instance
     float *out;                  // image 0 of the instance
     const float *base;
@@ -781,7 +786,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     if (tid == 0) abort_flag = 0;
     __syncthreads();
 
-    // warp 0: copies of view v into buffer buf (lane i moves line i's entries)
+    // one warp: copies of view v into buffer buf (lane i moves line i's entries)
+    const int tile = (r0 / kTile) * tiles_x(&g) + c0 / kTile, ntiles = tiles_n(&g);
     auto issue = [&](int v, int buf) {
         const DdView2 vwv = it.views[v];
         const int xbv = vwv.xb;
@@ -797,16 +803,13 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             elo = lo;
             ne = (hi - lo + 1) & ~1;
         }
-        int kmin, kmax;
-        tile_bin_range(GEOM, g, vwv, it.angles[v], c0, r0, &kmin, &kmax);
-        const int kb = kmin & ~1;
-        int kn = (kmax - kb + 2) & ~1;
-        if (kb + kn > rsd) kn = rsd - kb;
-        if (kn > kStage || kn <= 0) kn = 0;
+        const int2 tr = it.trange[(size_t)v * ntiles + tile];
+        const int kb = tr.x, kn = tr.y;
         if (lane == 0) {
             krange[4 * buf] = kb;
             krange[4 * buf + 1] = kn;
             krange[4 * buf + 2] = elo;
+            krange[4 * buf + 3] = xbv;
             dd_mbar_expect_tx(&bar[buf], (uint32_t)((nlines * ne + nb * kn) * (int)sizeof(int2) + kTile * (int)sizeof(float)));
         }
         __syncwarp();
@@ -830,7 +833,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     int inflight = -1;
     for (int v = 0; v < V; v++) {
         const int buf = v & 1;
-        if (warp == 0 && v + 1 < V) issue(v + 1, buf ^ 1);
+        // the issuing warp rotates so that no warp carries every view's copies
+        if (warp == (v & (kWarps - 1)) && v + 1 < V) issue(v + 1, buf ^ 1);
         if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
         uses[buf]++;
         __syncthreads();
@@ -838,9 +842,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             inflight = (v + 1 < V) ? (buf ^ 1) : -1;
             break;
         }
-        const DdView2 vw = it.views[v];
-        const int xb = vw.xb;
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
+        const int xb = krange[4 * buf + 3];
         const int2 *mp = mapb + (size_t)buf * kTile * kMapE;
         const float2 *sb = stage + (size_t)buf * kBI * kStage;
 #pragma unroll
@@ -859,6 +862,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             if (up.x < 0 || low.x < 0) continue;
             float wgt = (OPK == 0) ? 1.0f : alb[buf * kTile + lr];
             if (OPK == 2) {
+                const DdView2 vw = it.views[v];
                 const int line = xb ? r : c, pi = xb ? c : H - 1 - r;
                 float pcx, pcy;
                 if (xb) {
