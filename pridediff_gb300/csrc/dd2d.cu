@@ -160,6 +160,10 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
 }
 
 // Single-geometry forward launch: grid (views, image groups).
+// images per CTA of the single-geometry forward: fewer images per CTA keep
+// the double-buffered line tables small enough for more resident CTAs
+constexpr int kFwdImages = 4;
+
 template <int GEOM, int WEIGHTED, int NPASS>
 __global__ void __launch_bounds__(kThreads)
 k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ views,
@@ -169,14 +173,14 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, kFwdImages);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     uint32_t uses[2] = {0u, 0u};
     FwdItem it;
     it.v = blockIdx.x;
-    it.b0 = blockIdx.y * kBI;
-    it.nb = min(kBI, B - it.b0);
+    it.b0 = blockIdx.y * kFwdImages;
+    it.nb = min(kFwdImages, B - it.b0);
     it.V = V;
     it.nl = nl;
     it.views = views;
@@ -188,7 +192,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED, NPASS>(g, op, it, smem, g.num_det, rsmax, uses) && threadIdx.x == 0)
+    if (!fwd_view<GEOM, WEIGHTED, NPASS, kFwdImages>(g, op, it, smem, g.num_det, rsmax, uses) && threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
@@ -397,8 +401,8 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
                       int V, const float2 *tx, const float2 *ty, float *out, const float *sub,
                       int *status, cudaStream_t st) {
     const int rsmax = rs_entries(g->width > g->height ? g->width : g->height);
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax);
-    dim3 grid(V, (B + kBI - 1) / kBI);
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages);
+    dim3 grid(V, (B + kFwdImages - 1) / kFwdImages);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const float *bc = (const float *)(planb + P.bcoef);

@@ -139,13 +139,13 @@ struct FwdSmem {
     int rec, drec, tab, kt, dp, bar, total;
 };
 
-__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax) {
+__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI) {
     FwdSmem s;
     int o = 0;
     s.rec = o; o += 2 * (int)sizeof(DdLine);
     s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * (int)sizeof(DdLine);
-    s.tab = o; o += 2 * kBI * rsmax * (int)sizeof(float2);
-    s.kt = o; o += kBI * 32 * (int)sizeof(float) * 2;   // K for pixel pieces (x2 for para det)
+    s.tab = o; o += 2 * bi * rsmax * (int)sizeof(float2);
+    s.kt = o; o += bi * 32 * (int)sizeof(float) * 2;   // K for pixel pieces (x2 for para det)
     s.dp = o; o += ((D + 1 + 3) & ~3) * (int)sizeof(float);
     s.bar = o; o += 2 * (int)sizeof(uint64_t);
     s.total = (o + 127) & ~127;
@@ -177,7 +177,7 @@ __host__ __device__ inline int npass_class(int D) {
 // initialised bar[0..1]; `uses` counts completed phases per barrier so that a
 // persistent CTA can run many items back to back.  Returns false if a
 // bounded wait timed out (copies in flight have been drained).
-template <int GEOM, int WEIGHTED, int NPASS>
+template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, uint32_t *uses) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
@@ -188,7 +188,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     const int nline = xb ? g.height : g.width;
     const int npix = xb ? g.width : g.height;
     const int rs = rs_entries(npix);
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI);
     DdLine *rec = reinterpret_cast<DdLine *>(smem + L.rec);
     DdLine *drec = reinterpret_cast<DdLine *>(smem + L.drec);
     float2 *tab = reinterpret_cast<float2 *>(smem + L.tab);
@@ -215,17 +215,17 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         if (GEOM == DD_GEOM_PARA)
             dd_bulk_g2s(drec + buf, it.dlines + (size_t)v * it.nl + line, rec_bytes, &bar[buf]);
         for (int b = 0; b < nb; b++)
-            dd_bulk_g2s(tab + ((size_t)buf * kBI + b) * rsmax,
+            dd_bulk_g2s(tab + ((size_t)buf * BI + b) * rsmax,
                         tsrc + (size_t)(b0 + b) * img_stride + (size_t)line * rs, tab_bytes, &bar[buf]);
     };
 
     const int npass = (D + kWarps * kBinsPerWarp - 1) / (kWarps * kBinsPerWarp);
     constexpr int kMaxPass = NPASS;   // D <= NPASS * 248 detector bins
-    float acc[kMaxPass][kBI];
+    float acc[kMaxPass][BI];
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++)
 #pragma unroll
-        for (int b = 0; b < kBI; b++) acc[m][b] = 0.0f;
+        for (int b = 0; b < BI; b++) acc[m][b] = 0.0f;
 
     const float para_beta = xb ? FDIV(g.pix_y, g.det_size) : FDIV(g.pix_x, g.det_size);
     if (tid == 0) issue(0, 0);
@@ -247,7 +247,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             // BackProjTransWeighted: multiply every pixel by its FBP weight at
             // this view (FanFlatDisCPU2d.cpp:693, FanArcDisCPU2d.cpp:703) and
             // rebuild the line's prefix table in place (block scan).
-            float2 *tw = tab + (size_t)buf * kBI * rsmax;
+            float2 *tw = tab + (size_t)buf * BI * rsmax;
             const float lpos = xb
                 ? (float)(((double)g.height / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift)
                 : (float)(((double)line - g.width / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
@@ -304,7 +304,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             }
         }
         if (np > 0) {
-            const float2 *tb = tab + (size_t)buf * kBI * rsmax;
+            const float2 *tb = tab + (size_t)buf * BI * rsmax;
             for (int b = warp; b < nb; b += kWarps) kt[b * 32 + lane] = piece_K(R, tb + (size_t)b * rsmax, lane);
             __syncthreads();
             const float scale = (op == DD_OP_PROJ) ? 1.0f : R.h.alpha;
@@ -328,7 +328,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                 u = fminf(fmaxf(u, bound0), endv);
                 const Loc lc = locate(R, u);
 #pragma unroll
-                for (int b = 0; b < kBI; b++) {
+                for (int b = 0; b < BI; b++) {
                     if (b < nb) {
                         const float2 e = tb[(size_t)b * rsmax + lc.j];
                         const float f = fmaf(lc.r, e.y, fmaf(lc.dl, e.x, kt[b * 32 + lc.p]));
