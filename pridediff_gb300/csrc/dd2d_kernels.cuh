@@ -17,7 +17,7 @@ namespace dd2 {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kBinsPerWarp = 31;   // 32 boundaries -> 31 bins per warp pass
-constexpr int kBI = 8;             // images per CTA (geometry amortised over them)
+constexpr int kBI = 4;             // images per CTA (geometry amortised over them)
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n+1 float2, 16-B rows
