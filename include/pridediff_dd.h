@@ -184,6 +184,23 @@ DD_NAMED2D(BackProjParaDis2d);              /* RadonTorch.cpp:502  */
 DD_NAMED2D(BackProjTransParaDis2d);         /* RadonTorch.cpp:536  */
 #undef DD_NAMED2D
 
+/* ---- 2-D: system matrix ----------------------------------------------------
+ * Replaces GetSysMatrixPara2d / GetSysMatrixFanFlat2d / GetSysMatrixFanArc2d
+ * (RadonTorch.cpp:1270-1372): the COO matrix (V*D x H*W) with one entry per
+ * step of the DD merge walk, in the reference's order (view, walked line,
+ * step).  The reference builds it on the CPU; here it is built on the device
+ * in two passes over a plan from dd2d_plan:
+ *   1. dd2d_sysmatrix_count writes the entries of each (view, walked line)
+ *      into counts[dd2d_sysmatrix_lines()], index view * max(H, W) + line;
+ *   2. the caller takes the exclusive prefix sum of counts as offsets and
+ *      allocates nnz = sum(counts) rows / cols (int64) and vals (FP32);
+ *   3. dd2d_sysmatrix_fill writes the entries. */
+size_t dd2d_sysmatrix_lines(const dd_geom2d *g, int num_view);
+int dd2d_sysmatrix_count(int scan, const dd_geom2d *g, const void *plan, int num_view, long long *counts,
+                         dd_stream_t stream);
+int dd2d_sysmatrix_fill(int scan, const dd_geom2d *g, const void *plan, int num_view, const long long *offsets,
+                        long long *rows, long long *cols, float *vals, dd_stream_t stream);
+
 /* ---- 3-D: cone-flat, cone-arc, spiral --------------------------------------
  * Same conventions as 2-D.  source_pos is the spiral source table (4, V) on
  * the device (RadonTorch.cpp:1040-1043); pass NULL for the cone geometries.

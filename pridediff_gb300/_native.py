@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_BUILD, "libpridediff_dd.so")
 INCLUDE = os.path.join(_ROOT, "include")
 
 # translation units of the library (compiled in parallel)
-SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd3d.cu", "dd2d_noalloc.cu"]
+SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd2d_sysmat.cu", "dd3d.cu", "dd2d_noalloc.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -147,6 +147,13 @@ def _declare(lib):
     lib.dd2d_batch_status.argtypes = [i, ip, i, vp, ctypes.POINTER(ctypes.c_int)]
     lib.dd2d_validate.restype = i
     lib.dd2d_validate.argtypes = [i, i, g2, i, i]
+    lp = ctypes.POINTER(ctypes.c_longlong)
+    lib.dd2d_sysmatrix_lines.restype = sz
+    lib.dd2d_sysmatrix_lines.argtypes = [g2, i]
+    lib.dd2d_sysmatrix_count.restype = i
+    lib.dd2d_sysmatrix_count.argtypes = [i, g2, vp, i, vp, vp]
+    lib.dd2d_sysmatrix_fill.restype = i
+    lib.dd2d_sysmatrix_fill.argtypes = [i, g2, vp, i, vp, vp, vp, vp, vp]
     g3 = ctypes.POINTER(_Geom3d)
     lib.dd3d_validate.restype = i
     lib.dd3d_validate.argtypes = [i, i, g3, i, i]

@@ -91,13 +91,17 @@ DD_HD void dd_view2_setup(int geom, const dd_geom2d *g, float view, DdView2 *vw,
     for (int k = 0; k < g->num_det; k++) bcoef[k] = dd_view2_bcoef(g, vw, dp[k], dp[k + 1]);
 }
 
-// Per-line set-up: start of the walk and the drifted pixel boundaries.
-// `L` receives the pixel-side record; for the parallel beam `Ld` receives the
-// drifted detector-side record (may be NULL otherwise).
-// Para: ParaDisCPU2d.cpp:62-77.  Flat: FanFlatDisCPU2d.cpp:95-113.
-// Arc: FanArcDisCPU2d.cpp:97-120.
-DD_HD void dd_line2_setup(int geom, const dd_geom2d *g, float view, const DdView2 *vw,
-                          const float *dp, int line, DdLine *L, DdLine *Ld) {
+// Start of the walk of one line: first pixel boundary p0 and pixel pitch
+// pint on the projection axis, walk start bound0, first pixel i0 and first
+// detector bin idet0 (ParaDisCPU2d.cpp:62-77, FanFlatDisCPU2d.cpp:95-113,
+// FanArcDisCPU2d.cpp:97-120).
+struct DdLineStart {
+    float p0, pint, bound0;
+    int i0, idet0;
+};
+
+DD_HD void dd_line2_start(int geom, const dd_geom2d *g, float view, const DdView2 *vw,
+                          const float *dp, int line, DdLineStart *st) {
     const int W = g->width, H = g->height, D = g->num_det;
     const int xb = vw->xb;
     const int npix = xb ? W : H;
@@ -171,7 +175,24 @@ DD_HD void dd_line2_setup(int geom, const dd_geom2d *g, float view, const DdView
     }
     if (idet0 < 0) idet0 = 0;   // the reference indexes out of bounds there
     if (i0 < 0) i0 = 0;
+    st->p0 = p0;
+    st->pint = pint;
+    st->bound0 = bound0;
+    st->i0 = i0;
+    st->idet0 = idet0;
+}
 
+// Per-line set-up: start of the walk and the drifted pixel boundaries.
+// `L` receives the pixel-side record; for the parallel beam `Ld` receives the
+// drifted detector-side record (may be NULL otherwise).
+DD_HD void dd_line2_setup(int geom, const dd_geom2d *g, float view, const DdView2 *vw,
+                          const float *dp, int line, DdLine *L, DdLine *Ld) {
+    const int D = g->num_det;
+    const int npix = vw->xb ? g->width : g->height;
+    DdLineStart st;
+    dd_line2_start(geom, g, view, vw, dp, line, &st);
+    const float p0 = st.p0, pint = st.pint, bound0 = st.bound0;
+    const int i0 = st.i0, idet0 = st.idet0;
     DdLineHdr &h = L->h;
     h.bound0 = bound0;
     h.i0 = i0;
@@ -216,4 +237,55 @@ DD_HD void dd_line2_setup(int geom, const dd_geom2d *g, float view, const DdView
             dd_build_slots(Ld->p, hd.npiece, Ld->slot);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// System matrix of one walked line: the merge walk exactly as deeprecon's
+// CPU builders run it (GetSysMatrixPara2dKernel, ParaDisCPU2d.cpp:488-612;
+// GetSysMatrixFanFlat2dKernel, FanFlatDisCPU2d.cpp:1048-1216;
+// GetSysMatrixFanArc2dKernel, FanArcDisCPU2d.cpp:1057-), sequential FP32
+// recurrences included: one entry per step, row = view * D + detector bin
+// (reversed when the detector is flipped), column = pixel index in the image,
+// value = step width x bin scale.  With rows == NULL the entries are only
+// counted.  Returns the number of entries.  bcoef: the view's per-bin scales
+// (fan beams); dp: its boundary table (fan beams).
+// ---------------------------------------------------------------------------
+DD_HD long long dd_line2_sysmat(int geom, const dd_geom2d *g, float view, const DdView2 *vw, const float *dp,
+                                const float *bcoef, int v, int line, long long *rows, long long *cols,
+                                float *vals) {
+    const int W = g->width, H = g->height, D = g->num_det;
+    const int xb = vw->xb;
+    const int npix = xb ? W : H, nline = xb ? H : W;
+    if (line < 0 || line >= nline) return 0;
+    DdLineStart st;
+    dd_line2_start(geom, g, view, vw, dp, line, &st);
+    float b = st.bound0;
+    int ipix = st.i0, idet = st.idet0;
+    float point1 = FADD(FMUL((float)(ipix + 1), st.pint), st.p0);
+    float det1 = 0.0f;
+    if (geom == DD_GEOM_PARA) det1 = FADD(FMUL((float)(idet + 1), vw->di), vw->det0);
+    else if (idet < D) det1 = dp[idet + 1];
+    const float pbeta = xb ? FDIV(g->pix_y, g->det_size) : FDIV(g->pix_x, g->det_size);
+    long long n = 0;
+    while (ipix < npix && idet < D) {
+        const bool step_pix = point1 < det1;
+        if (rows) {
+            const float w = FSUB(step_pix ? point1 : det1, b);
+            rows[n] = (long long)v * D + (vw->flip ? D - 1 - idet : idet);
+            cols[n] = xb ? (long long)line * W + ipix : (long long)(H - 1 - ipix) * W + line;
+            vals[n] = FMUL(w, geom == DD_GEOM_PARA ? pbeta : bcoef[idet]);
+        }
+        n++;
+        if (step_pix) {
+            b = point1;
+            ipix++;
+            point1 = FADD(point1, st.pint);
+        } else {
+            b = det1;
+            idet++;
+            if (geom == DD_GEOM_PARA) det1 = FADD(det1, vw->di);
+            else if (idet < D) det1 = dp[idet + 1];
+        }
+    }
+    return n;
 }

@@ -210,13 +210,6 @@ def _apply3d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor,
     return out
 
 
-def _not_yet(name):
-    def f(*args, **kwargs):
-        raise NotImplementedError(f"radontorch.{name} is not available in this build")
-    f.__name__ = name
-    return f
-
-
 # ---------------------------------------------------------------------------
 # 2-D operators (RadonTorch.cpp:1376-1393)
 # ---------------------------------------------------------------------------
@@ -269,8 +262,55 @@ for _geo, _s in (("ConeFlat", "cone_flat"), ("ConeArc", "cone_arc"), ("Spiral", 
 # ---------------------------------------------------------------------------
 # System matrices (RadonTorch.cpp:1270-1372)
 # ---------------------------------------------------------------------------
-for _name in ("GetSysMatrixFanFlat2d", "GetSysMatrixFanArc2d", "GetSysMatrixPara2d"):
-    globals()[_name] = _not_yet(_name)
+def _sysmatrix(scan: str, options, angles: torch.Tensor) -> torch.Tensor:
+    """COO system matrix (V*D x H*W) of a 2-D geometry, built on the GPU.
+
+    Same entries, order and CPU sparse result as deeprecon's builders (one
+    entry per step of the DD merge walk, view by view and line by line).  The
+    reference accepts CPU tensors only (its Python wrapper moves them there,
+    function.py:535-553); here CPU and CUDA inputs are both accepted and the
+    work runs on the current CUDA device.
+    """
+    if not torch.cuda.is_available():
+        raise RuntimeError("pridediff_gb300 builds the system matrix on a CUDA device; none is available")
+    lib = N.load()
+    g = N.geom2d(host_options(options))
+    dev = angles.device if angles.device.type == "cuda" else torch.device("cuda", torch.cuda.current_device())
+    ang = angles.detach().to(dev, torch.float32).contiguous()
+    V = int(ang.shape[0])
+    sc = N.SCAN2D[scan]
+    with torch.cuda.device(dev):
+        N.check(lib.dd2d_validate(sc, N.OPS["proj"], g, 1, V), f"{scan} system matrix")
+        plan = plan2d(scan, g, ang)
+        n_lines = int(lib.dd2d_sysmatrix_lines(g, V))
+        counts = torch.empty(n_lines, dtype=torch.int64, device=dev)
+        N.check(lib.dd2d_sysmatrix_count(sc, g, plan.data_ptr(), V, counts.data_ptr(), _stream_ptr(dev)),
+                f"{scan} system matrix")
+        offsets = torch.cumsum(counts, 0) - counts
+        nnz = int(counts.sum().item())
+        rows = torch.empty(max(nnz, 1), dtype=torch.int64, device=dev)
+        cols = torch.empty(max(nnz, 1), dtype=torch.int64, device=dev)
+        vals = torch.empty(max(nnz, 1), dtype=torch.float32, device=dev)
+        N.check(lib.dd2d_sysmatrix_fill(sc, g, plan.data_ptr(), V, offsets.data_ptr(), rows.data_ptr(),
+                                        cols.data_ptr(), vals.data_ptr(), _stream_ptr(dev)), f"{scan} system matrix")
+    indices = torch.stack([rows[:nnz], cols[:nnz]]).cpu()
+    return torch.sparse_coo_tensor(indices, vals[:nnz].cpu(), (V * g.num_det, g.height * g.width),
+                                   dtype=torch.float32)
+
+
+def GetSysMatrixFanFlat2d(options, angles):
+    """Replaces radontorch.GetSysMatrixFanFlat2d (deeprecon/interface/RadonTorch.cpp:1270)."""
+    return _sysmatrix("flat", options, angles)
+
+
+def GetSysMatrixFanArc2d(options, angles):
+    """Replaces radontorch.GetSysMatrixFanArc2d (deeprecon/interface/RadonTorch.cpp:1305)."""
+    return _sysmatrix("arc", options, angles)
+
+
+def GetSysMatrixPara2d(options, angles):
+    """Replaces radontorch.GetSysMatrixPara2d (deeprecon/interface/RadonTorch.cpp:1340)."""
+    return _sysmatrix("para", options, angles)
 
 NAMES2D = [n for n in globals() if n.endswith("Dis2d")]
 ALL_NAMES = NAMES2D + NAMES3D + ["GetSysMatrixFanFlat2d", "GetSysMatrixFanArc2d", "GetSysMatrixPara2d"]

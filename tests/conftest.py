@@ -44,6 +44,11 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def sysmat_golden():
+    return np.load(os.path.join(ROOT, "tests", "golden", "sysmat_golden.npz"))
+
+
+@pytest.fixture(scope="session")
 def oracle_mod():
     import oracle
     oracle.build()
@@ -83,6 +88,20 @@ class HostModel:
                                     out.ctypes.data_as(fp), a.ctypes.data_as(fp), B, V)
         assert rc == 0
         return out
+
+    def sysmatrix2d(self, geom, angles, opt):
+        """(rows, cols, vals) of the system matrix through the kernels' line walk."""
+        lp, fp = ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_float)
+        f = self.lib.model_sysmatrix2d
+        f.restype = ctypes.c_longlong
+        f.argtypes = [ctypes.c_int, ctypes.POINTER(_G2), fp, ctypes.c_int, lp, lp, fp]
+        g = _G2(int(opt[0]), int(opt[1]), int(opt[2]), *[float(v) for v in opt[3:]])
+        a = np.ascontiguousarray(angles, np.float32)
+        n = f(self.SCAN[geom], ctypes.byref(g), a.ctypes.data_as(fp), len(a), None, None, None)
+        rows, cols, vals = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n, np.float32)
+        f(self.SCAN[geom], ctypes.byref(g), a.ctypes.data_as(fp), len(a), rows.ctypes.data_as(lp),
+          cols.ctypes.data_as(lp), vals.ctypes.data_as(fp))
+        return rows, cols, vals
 
     def check_pieces(self, v0, pint, i0, nend):
         npc, fl, dev = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()

@@ -3,7 +3,8 @@
 Run in a checkout where the reference sources exist (they are compiled into
 oracle/_ref/libddref.so by `make -C oracle`):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py               # operator outputs -> dd2d_golden.npz
+    python tests/golden/make_golden.py --sysmatrix   # system matrices  -> sysmat_golden.npz
 
 Every case stores its seeded inputs and the reference outputs (computed by
 the unmodified deeprecon CPU projectors, single-threaded), so the tests can
@@ -80,5 +81,41 @@ def main():
     print("wrote", path, os.path.getsize(path) // 1024, "KB")
 
 
+# (name, geometry, options, angles) for the system matrices: small images so
+# that each COO matrix stays at a few thousand entries; views include the
+# 45-degree branch boundary and flipped detectors
+SYS_CASES = [
+    ("para_sys", "para", [20, 16, 27, 1.0, 1.1, 1.0, 500.0, 1000.0, 0.3, -0.2, 0.25],
+     np.concatenate([np.arange(10) * np.pi / 10, [np.pi / 4]])),
+    ("flat_sys", "flat", [20, 16, 25, 0.9, 0.8, 1.3, 595.0, 1085.6, 0.5, -0.4, 0.6],
+     np.concatenate([np.arange(12) * 2 * np.pi / 12, [np.pi / 4, 3 * np.pi / 4]])),
+    ("arc_sys", "arc", [20, 16, 25, 0.9, 0.8, 1.3 / 1085.6, 595.0, 1085.6, 0.5, -0.4, 0.6 / 1085.6],
+     np.concatenate([np.arange(12) * 2 * np.pi / 12, [np.pi / 4, 3 * np.pi / 4]])),
+]
+
+
+def main_sysmatrix():
+    """deeprecon's GetSysMatrix* COO matrices (rows, cols, vals in its order)."""
+    if not oracle.have_ref():
+        oracle.build()
+    if not oracle.have_ref():
+        raise SystemExit("reference sources not present: cannot regenerate golden vectors")
+    out = {}
+    for name, geom, opt, ang in SYS_CASES:
+        ang = np.asarray(ang, np.float32)
+        rows, cols, vals = oracle.ref_sysmatrix(geom, ang, opt)
+        out[f"{name}/options"] = np.asarray(opt, np.float32)
+        out[f"{name}/angles"] = ang
+        out[f"{name}/rows"] = rows
+        out[f"{name}/cols"] = cols
+        out[f"{name}/vals"] = vals
+    path = os.path.join(HERE, "sysmat_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path) // 1024, "KB")
+
+
 if __name__ == "__main__":
-    main()
+    if "--sysmatrix" in sys.argv[1:]:
+        main_sysmatrix()
+    else:
+        main()

@@ -266,3 +266,23 @@ extern "C" int model_check_pieces(float v0, float pint, int i0, int nend, int *n
     *maxdev_ulp = worst;
     return bad;
 }
+
+// System matrix through the kernels' line walk (dd_line2_sysmat), view by
+// view and line by line like deeprecon's builders.  With rows == NULL only
+// the number of entries is returned.
+extern "C" long long model_sysmatrix2d(int scan, const dd_geom2d *gp, const float *angles, int V, long long *rows,
+                                       long long *cols, float *vals) {
+    const dd_geom2d g = *gp;
+    const int geom = scan;
+    const int D = g.num_det, nl = g.height > g.width ? g.height : g.width;
+    std::vector<float> dp(D + 1), bc(D + 1);
+    long long n = 0;
+    for (int v = 0; v < V; v++) {
+        DdView2 vw;
+        dd_view2_setup(geom, &g, angles[v], &vw, dp.data(), bc.data());
+        for (int line = 0; line < nl; line++)
+            n += dd_line2_sysmat(geom, &g, angles[v], &vw, dp.data(), bc.data(), v, line, rows ? rows + n : nullptr,
+                                 rows ? cols + n : nullptr, rows ? vals + n : nullptr);
+    }
+    return n;
+}

@@ -205,3 +205,36 @@ def test_errors_are_raised():
     bad[3] = float("nan")
     with pytest.raises(RuntimeError):
         radontorch.ProjFanFlatDis2d(torch.zeros(1, 1, 64, 64, device="cuda"), bad, ang)
+
+
+@pytest.mark.parametrize("case", ["para_sys", "flat_sys", "arc_sys"])
+def test_gpu_sysmatrix_matches_reference(sysmat_golden, case):
+    """GetSysMatrix* built on the GPU against deeprecon's CPU builder: same
+    entries in the same order, values within FP32 rounding."""
+    from pridediff_gb300 import radontorch
+    geom = case.split("_")[0]
+    name = {"para": "GetSysMatrixPara2d", "flat": "GetSysMatrixFanFlat2d", "arc": "GetSysMatrixFanArc2d"}[geom]
+    opt = torch.tensor(sysmat_golden[f"{case}/options"])
+    ang = torch.tensor(sysmat_golden[f"{case}/angles"])
+    m = getattr(radontorch, name)(opt, ang)
+    assert m.is_sparse and m.device.type == "cpu" and m.dtype == torch.float32
+    W, H, D, V = int(opt[0]), int(opt[1]), int(opt[2]), len(ang)
+    assert tuple(m.shape) == (V * D, H * W)
+    idx, vals = m._indices().numpy(), m._values().numpy()
+    assert np.array_equal(idx[0], sysmat_golden[f"{case}/rows"])
+    assert np.array_equal(idx[1], sysmat_golden[f"{case}/cols"])
+    ref = sysmat_golden[f"{case}/vals"]
+    assert np.max(np.abs(vals - ref)) <= 1e-6 * max(1.0, float(np.max(np.abs(ref))))
+
+
+def test_gpu_sysmatrix_times_image_is_the_projection():
+    """The system matrix applied to an image equals the forward projection
+    (the parallel-beam configuration: 256^2, 180 views, 367 detectors)."""
+    from pridediff_gb300 import radontorch
+    opt = torch.tensor([256, 256, 367, 1.0, 1.0, 1.0, 500.0, 1000.0, 0.0, 0.0, 0.0])
+    ang = torch.arange(180, dtype=torch.float32) * (np.pi / 180)
+    m = radontorch.GetSysMatrixPara2d(opt, ang).coalesce()
+    x = _phantom(256, 256, 10, np.random.default_rng(3))
+    ax = torch.sparse.mm(m.double(), torch.from_numpy(x.reshape(-1, 1)).double()).numpy().reshape(180, 367)
+    ref = run("para", "proj", x[None], ang.numpy(), opt.numpy())[0]
+    assert rel_l2(ref, ax) <= 1e-6

@@ -55,3 +55,15 @@ def test_piece_model_edge_sequences(host_model):
                         (-256.0, 0.3, 2000), (-0.001, 0.001, 50), (5.0, 2.0, 1)]:
         bad, npiece, flags, dev = host_model.check_pieces(float(np.float32(v0)), float(np.float32(pint)), 0, n)
         assert bad < 1000000 and dev <= 1.0 + 1e-6
+
+
+@pytest.mark.parametrize("case", ["para_sys", "flat_sys", "arc_sys"])
+def test_model_sysmatrix_matches_reference(sysmat_golden, host_model, case):
+    """The system-matrix line walk (dd_line2_sysmat) reproduces deeprecon's
+    GetSysMatrix* builders entry for entry: same order, rows, columns and
+    FP32 values."""
+    geom = case.split("_")[0]
+    rows, cols, vals = host_model.sysmatrix2d(geom, sysmat_golden[f"{case}/angles"], sysmat_golden[f"{case}/options"])
+    assert np.array_equal(rows, sysmat_golden[f"{case}/rows"])
+    assert np.array_equal(cols, sysmat_golden[f"{case}/cols"])
+    assert np.array_equal(vals, sysmat_golden[f"{case}/vals"])
