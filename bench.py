@@ -399,6 +399,7 @@ def main():
     dev = torch.device("cuda", local)
 
     import pridediff_gb300 as P
+    from pridediff_gb300.replicas import max_over_ranks
     lib = P._native.load()
 
     B, V = GEOM["batch"], GEOM["views"]
@@ -445,11 +446,7 @@ def main():
     wall = time.perf_counter() - wall0
     launches = (lib.dd_launch_count() - n0) // max(args.steps, 1)
     barrier()
-    ms = sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / args.steps, dev)
     value = world * B / (ms / 1e3)
 
     # ---- dominant kernel: live CUDA-event timing of each launch
@@ -491,11 +488,7 @@ def main():
         g_host.copy_(g, non_blocking=True)
         e_e[i].record()
     torch.cuda.synchronize()
-    e2e_ms = sum(a.elapsed_time(b) for a, b in zip(e_s, e_e)) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(e_s, e_e)) / args.steps, dev)
     e2e_value = world * B / (e2e_ms / 1e3)
 
     extras = None
