@@ -168,8 +168,8 @@ struct FwdItem {
 // Detector passes of a 256-thread CTA (8 warps x 31 bins each) rounded up to
 // the instantiated classes; NPASS sizes the per-thread accumulators, so a
 // smaller class means fewer registers and more resident CTAs per SM.
-__host__ __device__ inline int npass_class(int D) {
-    const int n = (D + kWarps * kBinsPerWarp - 1) / (kWarps * kBinsPerWarp);
+__host__ __device__ inline int npass_class(int D, int nw = kWarps) {
+    const int n = (D + nw * kBinsPerWarp - 1) / (nw * kBinsPerWarp);
     return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : 8;
 }
 
@@ -177,7 +177,7 @@ __host__ __device__ inline int npass_class(int D) {
 // initialised bar[0..1]; `uses` counts completed phases per barrier so that a
 // persistent CTA can run many items back to back.  Returns false if a
 // bounded wait timed out (copies in flight have been drained).
-template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI>
+template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, uint32_t *uses) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
@@ -196,7 +196,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     float *dps = reinterpret_cast<float *>(smem + L.dp);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     __shared__ int abort_flag;
-    __shared__ float wsum[kWarps];
+    __shared__ float wsum[NW];
 
     const float2 *tsrc = xb ? it.tabx : it.taby;
     const size_t img_stride = (size_t)nline * rs;          // float2 per image
@@ -206,7 +206,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
 
     if (tid == 0) abort_flag = 0;
     if (GEOM != DD_GEOM_PARA)
-        for (int k = tid; k <= D; k += kThreads) dps[k] = it.dp[(size_t)v * (D + 1) + k];
+        for (int k = tid; k <= D; k += (NW * 32)) dps[k] = it.dp[(size_t)v * (D + 1) + k];
     __syncthreads();
 
     auto issue = [&](int line, int buf) {
@@ -219,7 +219,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                         tsrc + (size_t)(b0 + b) * img_stride + (size_t)line * rs, tab_bytes, &bar[buf]);
     };
 
-    const int npass = (D + kWarps * kBinsPerWarp - 1) / (kWarps * kBinsPerWarp);
+    const int npass = (D + NW * kBinsPerWarp - 1) / (NW * kBinsPerWarp);
     constexpr int kMaxPass = NPASS;   // D <= NPASS * 248 detector bins
     float acc[kMaxPass][BI];
 #pragma unroll
@@ -254,7 +254,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             for (int b = 0; b < nb; b++) {
                 float2 *t = tw + (size_t)b * rsmax;
                 constexpr int kPer = 16;   // npix <= 4096
-                const int per = (npix + kThreads - 1) / kThreads;
+                const int per = (npix + (NW * 32) - 1) / (NW * 32);
                 float yv[kPer];
                 float run = 0.0f;
 #pragma unroll
@@ -295,9 +295,9 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                         pre += yv[q];
                     }
                 }
-                if (tid == kThreads - 1) {
+                if (tid == (NW * 32) - 1) {
                     float tot = 0.0f;
-                    for (int w = 0; w < kWarps; w++) tot += wsum[w];
+                    for (int w = 0; w < NW; w++) tot += wsum[w];
                     t[npix] = make_float2(tot, 0.0f);
                 }
                 __syncthreads();
@@ -305,7 +305,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         }
         if (np > 0) {
             const float2 *tb = tab + (size_t)buf * BI * rsmax;
-            for (int b = warp; b < nb; b += kWarps) kt[b * 32 + lane] = piece_K(R, tb + (size_t)b * rsmax, lane);
+            for (int b = warp; b < nb; b += NW) kt[b * 32 + lane] = piece_K(R, tb + (size_t)b * rsmax, lane);
             __syncthreads();
             const float scale = (op == DD_OP_PROJ) ? 1.0f : R.h.alpha;
             const float bound0 = R.h.bound0, endv = R.h.endv;
@@ -313,7 +313,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
 #pragma unroll
             for (int m = 0; m < kMaxPass; m++) {
                 if (m >= npass) break;
-                const int kb = m * (kWarps * kBinsPerWarp) + warp * kBinsPerWarp + lane;
+                const int kb = m * (NW * kBinsPerWarp) + warp * kBinsPerWarp + lane;
                 float u;
                 if (kb <= idet0) {
                     u = bound0;   // lower boundary of bin idet0 is the walk start
@@ -352,7 +352,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++) {
         if (m >= npass) break;
-        const int k = m * (kWarps * kBinsPerWarp) + warp * kBinsPerWarp + lane;
+        const int k = m * (NW * kBinsPerWarp) + warp * kBinsPerWarp + lane;
         if (lane < kBinsPerWarp && k < D) {
             float beta = 1.0f;
             if (op == DD_OP_PROJ) beta = (GEOM == DD_GEOM_PARA) ? para_beta : it.bcoef[(size_t)v * (D + 1) + k];
