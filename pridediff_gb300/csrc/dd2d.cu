@@ -271,8 +271,8 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const float *__restrict__ base, float scale, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
-    init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar));
-    uint32_t uses[2] = {0u, 0u};
+    init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
+    uint32_t uses[kAdjBufs] = {0u, 0u, 0u};
     AdjItem it;
     it.c0 = blockIdx.x * kTile;
     it.r0 = blockIdx.y * kTile;

@@ -247,8 +247,8 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
-    init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar));
-    uint32_t uses[2] = {0u, 0u};
+    init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
+    uint32_t uses[kAdjBufs] = {0u, 0u, 0u};
     for (;;) {
         const int i = next_item(counter + 1);
         if (i >= nitems) break;

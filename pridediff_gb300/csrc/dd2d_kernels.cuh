@@ -326,6 +326,9 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                     u = dps[min(kb, D)];
                 }
                 u = fminf(fmaxf(u, bound0), endv);
+                // 32 boundaries clamped to the same end of the walk give 31
+                // zero differences: the warp skips the bins this line misses
+                if (__all_sync(0xffffffffu, u == bound0) || __all_sync(0xffffffffu, u == endv)) continue;
                 const Loc lc = locate(R, u);
 #pragma unroll
                 for (int b = 0; b < BI; b++) {
@@ -370,10 +373,9 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     return true;
 }
 
-__device__ __forceinline__ void init_bars(uint64_t *bar) {
+__device__ __forceinline__ void init_bars(uint64_t *bar, int n = 2) {
     if (threadIdx.x == 0) {
-        dd_mbar_init(&bar[0], 1);
-        dd_mbar_init(&bar[1], 1);
+        for (int i = 0; i < n; i++) dd_mbar_init(&bar[i], 1);
         dd_fence_mbar_init();
     }
     __syncthreads();
@@ -421,6 +423,9 @@ constexpr int kStage = 256;
 // Staged adjoint-map entries per line and view: the boundaries of a 32-pixel
 // run plus one below it, from an even first entry.
 constexpr int kMapE = 36;
+// Views in flight in the fan-beam adjoint: the copies of view v + 2 are issued
+// while view v is computed (part of the map comes from HBM).
+constexpr int kAdjBufs = 3;
 
 // Shared-memory layout of the adjoint kernel (bytes).  Parallel beam: line
 // records (and detector-side records); fan beams: adjoint-map rows, detector
@@ -436,11 +441,11 @@ __host__ __device__ inline AdjSmem adj_smem(int geom) {
     s.map = s.alpha = 0;
     if (geom != DD_GEOM_PARA) {
         s.rec = s.drec = s.kd = 0;
-        s.map = o; o += 2 * kTile * kMapE * (int)sizeof(int2);
-        s.stage = o; o += 2 * kBI * kStage * (int)sizeof(float2);
-        s.alpha = o; o += 2 * kTile * (int)sizeof(float);
-        s.krange = o; o += 8 * (int)sizeof(int);
-        s.bar = o; o += 2 * (int)sizeof(uint64_t);
+        s.map = o; o += kAdjBufs * kTile * kMapE * (int)sizeof(int2);
+        s.stage = o; o += kAdjBufs * kBI * kStage * (int)sizeof(float2);
+        s.alpha = o; o += kAdjBufs * kTile * (int)sizeof(float);
+        s.krange = o; o += 4 * kAdjBufs * (int)sizeof(int);
+        s.bar = o; o += kAdjBufs * (int)sizeof(uint64_t);
         s.total = (o + 127) & ~127;
         return s;
     }
@@ -829,17 +834,21 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
 #pragma unroll
         for (int b = 0; b < kBI; b++) acc[q][b] = 0.0f;
 
-    if (warp == 0) issue(0, 0);
-    int inflight = -1;
+    if (warp == 0) {
+        issue(0, 0);
+        if (V > 1) issue(1, 1);
+    }
+    int vstop = V;   // first view not waited for (copies of vstop, vstop+1 may be in flight)
     for (int v = 0; v < V; v++) {
-        const int buf = v & 1;
+        const int buf = v % kAdjBufs;
+        // the copies of view v + 2 go into the buffer view v - 1 has released;
         // the issuing warp rotates so that no warp carries every view's copies
-        if (warp == (v & (kWarps - 1)) && v + 1 < V) issue(v + 1, buf ^ 1);
+        if (warp == (v & (kWarps - 1)) && v + 2 < V) issue(v + 2, (v + 2) % kAdjBufs);
         if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
         uses[buf]++;
         __syncthreads();
         if (abort_flag) {
-            inflight = (v + 1 < V) ? (buf ^ 1) : -1;
+            vstop = v + 1;
             break;
         }
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
@@ -892,8 +901,12 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
     if (abort_flag) {
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
-        if (inflight >= 0) uses[inflight]++;
+        // let the copies of views vstop and vstop + 1 (issued, not waited for) land
+        for (int u = vstop; u < V && u < vstop + 2; u++) {
+            const int b = u % kAdjBufs;
+            if (tid == 0) dd_mbar_wait(&bar[b], uses[b] & 1);
+            uses[b]++;
+        }
         __syncthreads();
         return false;
     }
