@@ -838,19 +838,20 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         issue(0, 0);
         if (V > 1) issue(1, 1);
     }
-    int vstop = V;   // first view not waited for (copies of vstop, vstop+1 may be in flight)
+    int vstop = V;   // first view not waited for (the copies of vstop may be in flight)
     for (int v = 0; v < V; v++) {
         const int buf = v % kAdjBufs;
-        // the copies of view v + 2 go into the buffer view v - 1 has released;
-        // the issuing warp rotates so that no warp carries every view's copies
-        if (warp == (v & (kWarps - 1)) && v + 2 < V) issue(v + 2, (v + 2) % kAdjBufs);
         if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
         uses[buf]++;
+        // one barrier per view: past it every warp has finished view v - 1
         __syncthreads();
         if (abort_flag) {
             vstop = v + 1;
             break;
         }
+        // so the copies of view v + 2 can go into the buffer of view v - 1; the
+        // issuing warp rotates so that no warp carries every view's copies
+        if (warp == (v & (kWarps - 1)) && v + 2 < V) issue(v + 2, (v + 2) % kAdjBufs);
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
         const int xb = krange[4 * buf + 3];
         const int2 *mp = mapb + (size_t)buf * kTile * kMapE;
@@ -887,22 +888,34 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             const float offU = __int_as_float(up.y), offL = __int_as_float(low.y);
             const bool inU = (unsigned)(up.x - kb) < (unsigned)kn;
             const bool inL = (unsigned)(low.x - kb) < (unsigned)kn;
+            if (inU && inL) {   // both entries in the staged slice (the usual case)
+                const float2 *su = sb + (up.x - kb), *sl = sb + (low.x - kb);
 #pragma unroll
-            for (int b = 0; b < kBI; b++) {
-                if (b >= nb) break;
-                const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
-                const float2 e = inU ? sb[b * kStage + (up.x - kb)] : __ldg(t + up.x);
-                const float2 e2 = inL ? sb[b * kStage + (low.x - kb)] : __ldg(t + low.x);
-                const float hu = fmaf(offU, e.y, e.x);
-                const float hl = fmaf(offL, e2.y, e2.x);
-                acc[q][b] += wgt * (hu - hl);
+                for (int b = 0; b < kBI; b++) {
+                    if (b >= nb) break;
+                    const float2 e = su[b * kStage], e2 = sl[b * kStage];
+                    const float hu = fmaf(offU, e.y, e.x);
+                    const float hl = fmaf(offL, e2.y, e2.x);
+                    acc[q][b] += wgt * (hu - hl);
+                }
+            } else {
+#pragma unroll
+                for (int b = 0; b < kBI; b++) {
+                    if (b >= nb) break;
+                    const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
+                    const float2 e = inU ? sb[b * kStage + (up.x - kb)] : __ldg(t + up.x);
+                    const float2 e2 = inL ? sb[b * kStage + (low.x - kb)] : __ldg(t + low.x);
+                    const float hu = fmaf(offU, e.y, e.x);
+                    const float hl = fmaf(offL, e2.y, e2.x);
+                    acc[q][b] += wgt * (hu - hl);
+                }
             }
         }
-        __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
+    __syncthreads();   // the next item's first copies reuse the buffers
     if (abort_flag) {
-        // let the copies of views vstop and vstop + 1 (issued, not waited for) land
-        for (int u = vstop; u < V && u < vstop + 2; u++) {
+        // let the copies of view vstop (issued, not waited for) land
+        for (int u = vstop; u < V && u < vstop + 1; u++) {
             const int b = u % kAdjBufs;
             if (tid == 0) dd_mbar_wait(&bar[b], uses[b] & 1);
             uses[b]++;
