@@ -229,18 +229,15 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
 
     const float para_beta = xb ? FDIV(g.pix_y, g.det_size) : FDIV(g.pix_x, g.det_size);
     if (tid == 0) issue(0, 0);
-    int inflight = 0;   // buffer whose copy is outstanding
     for (int line = 0; line < nline; line++) {
         const int buf = line & 1;
-        if (tid == 0 && line + 1 < nline) issue(line + 1, buf ^ 1);
-        inflight = buf;
         if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
         uses[buf]++;
+        // past this barrier every warp has finished line - 1, whose buffer
+        // takes the copies of line + 1
         __syncthreads();
-        if (abort_flag) {
-            inflight = (line + 1 < nline) ? (buf ^ 1) : -1;
-            break;
-        }
+        if (abort_flag) break;
+        if (tid == 0 && line + 1 < nline) issue(line + 1, buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
         if (WEIGHTED && np > 0) {
@@ -341,17 +338,11 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                 }
             }
         }
-        __syncthreads();
     }
-    if (abort_flag) {
-        // let a copy still in flight land before the buffers are reused or freed
-        if (tid == 0 && inflight >= 0) {
-            dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
-        }
-        if (inflight >= 0) uses[inflight]++;
-        __syncthreads();
-        return false;
-    }
+    // no copy is left in flight here: the next line's copies are issued only
+    // after its predecessor's wait succeeded
+    __syncthreads();   // the next item's first copies reuse the buffers
+    if (abort_flag) return false;
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++) {
         if (m >= npass) break;
