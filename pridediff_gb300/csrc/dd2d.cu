@@ -180,7 +180,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, kFwdImages);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
-    uint32_t uses[2] = {0u, 0u};
+    DdPhases ph;
     FwdItem it;
     it.v = blockIdx.x;
     it.b0 = blockIdx.y * kFwdImages;
@@ -196,7 +196,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED, NPASS, kFwdImages, NW>(g, op, it, smem, g.num_det, rsmax, uses) && threadIdx.x == 0)
+    if (!fwd_view<GEOM, WEIGHTED, NPASS, kFwdImages, NW>(g, op, it, smem, g.num_det, rsmax, ph) && threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
@@ -257,7 +257,7 @@ k_trange(dd_geom2d g, int V, const DdView2 *__restrict__ views, const float *__r
     int kn = (kmax - kb + 2) & ~1;
     if (kb + kn > rsd) kn = rsd - kb;
     if (kn > kStage || kn <= 0) kn = 0;
-    trange[i] = make_int2(kb, kn);
+    trange[i] = make_int2(kb, kn | (views[v].xb ? 1 << 16 : 0));   // the view's axis in bit 16
 }
 
 // Single-geometry adjoint launch: grid (tiles x, tiles y, image groups).
@@ -272,7 +272,7 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
     init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
-    uint32_t uses[kAdjBufs] = {0u, 0u, 0u};
+    DdPhases ph;
     AdjItem it;
     it.c0 = blockIdx.x * kTile;
     it.r0 = blockIdx.y * kTile;
@@ -293,8 +293,8 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     it.base = base;
     it.scale = scale;
     bool ok;
-    if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(g, it, smem, uses);
-    else ok = adj_tile_map<GEOM, OPK>(g, it, smem, uses);
+    if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(g, it, smem, ph);
+    else ok = adj_tile_map<GEOM, OPK>(g, it, smem, ph);
     if (!ok && threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
 }
 

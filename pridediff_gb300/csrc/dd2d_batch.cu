@@ -210,7 +210,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
     extern __shared__ __align__(128) unsigned char smem[];
     const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
-    uint32_t uses[2] = {0u, 0u};
+    DdPhases ph;
     for (;;) {
         const int i = next_item(counter);
         if (i >= nitems) break;
@@ -232,7 +232,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
         it.taby = tabs + d.taby_off;
         it.out = out + d.sino_off;
         it.sub = sub ? sub + d.sino_off : nullptr;
-        if (!fwd_view<GEOM, 0, NPASS>(d.g, op, it, smem, Dmax, rsmax, uses)) {
+        if (!fwd_view<GEOM, 0, NPASS>(d.g, op, it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }
@@ -248,7 +248,7 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
     init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
-    uint32_t uses[kAdjBufs] = {0u, 0u, 0u};
+    DdPhases ph;
     for (;;) {
         const int i = next_item(counter + 1);
         if (i >= nitems) break;
@@ -275,8 +275,8 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
         it.base = base ? base + d.img_off : nullptr;
         it.scale = scale;
         bool ok;
-        if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(d.g, it, smem, uses);
-        else ok = adj_tile_map<GEOM, OPK>(d.g, it, smem, uses);
+        if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(d.g, it, smem, ph);
+        else ok = adj_tile_map<GEOM, OPK>(d.g, it, smem, ph);
         if (!ok) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;

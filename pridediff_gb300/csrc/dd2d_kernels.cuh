@@ -174,12 +174,12 @@ __host__ __device__ inline int npass_class(int D, int nw = kWarps) {
 }
 
 // Forward (detector-gather) evaluation of one work item.  The caller has
-// initialised bar[0..1]; `uses` counts completed phases per barrier so that a
+// initialised bar[0..1]; `ph` tracks the barriers' phases so that a
 // persistent CTA can run many items back to back.  Returns false if a
 // bounded wait timed out (copies in flight have been drained).
 template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
-                         int Dmax, int rsmax, uint32_t *uses) {
+                         int Dmax, int rsmax, DdPhases &ph) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int D = g.num_det;
@@ -231,8 +231,8 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     if (tid == 0) issue(0, 0);
     for (int line = 0; line < nline; line++) {
         const int buf = line & 1;
-        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
-        uses[buf]++;
+        if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
+        ph.flip(buf);
         // past this barrier every warp has finished line - 1, whose buffer
         // takes the copies of line + 1
         __syncthreads();
@@ -513,7 +513,7 @@ struct AdjItem {
     const DdLine *lines, *dlines;
     const int2 *amap;            // fan beams: adjoint map (plan)
     const float *alpha;          // fan beams: per-line DD-BP scales (plan)
-    const int2 *trange;          // fan beams: staged detector-table slice per (view, tile) (plan)
+    const int2 *trange;          // fan beams, per (view, tile): {first staged bin, bins | xb << 16} (plan)
     const float2 *dtab;          // detector tables of image 0 of the instance
     float *out;                  // image 0 of the instance
     const float *base;
@@ -521,7 +521,7 @@ struct AdjItem {
 };
 
 template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
-__device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, uint32_t *uses) {
+__device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, DdPhases &ph) {
     const AdjSmem SL = adj_smem(GEOM);
     const int V = it.V, nl = it.nl;
     const float *__restrict__ angles = it.angles;
@@ -592,8 +592,8 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
     for (int v = 0; v < V; v++) {
         const int buf = v & 1;
         if (tid == 0 && v + 1 < V) issue(v + 1, buf ^ 1);
-        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
-        uses[buf]++;
+        if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
+        ph.flip(buf);
         __syncthreads();
         if (abort_flag) {
             inflight = (v + 1 < V) ? (buf ^ 1) : -1;
@@ -722,8 +722,8 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
         __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
     if (abort_flag) {
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
-        if (inflight >= 0) uses[inflight]++;
+        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], ph.parity(inflight));
+        if (inflight >= 0) ph.flip(inflight);
         __syncthreads();
         return false;
     }
@@ -765,7 +765,7 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
 // H(u) = G_k + (u - d_k) g_k read at the two staged boundary entries.
 // ---------------------------------------------------------------------------
 template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
-__device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, uint32_t *uses) {
+__device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, DdPhases &ph) {
     const AdjSmem SL = adj_smem(GEOM);
     const int V = it.V, nl = it.nl;
     const int W = g.width, H = g.height, D = g.num_det;
@@ -784,9 +784,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
 
     // one warp: copies of view v into buffer buf (lane i moves line i's entries)
     const int tile = (r0 / kTile) * tiles_x(&g) + c0 / kTile, ntiles = tiles_n(&g);
-    auto issue = [&](int v, int buf) {
-        const DdView2 vwv = it.views[v];
-        const int xbv = vwv.xb;
+    auto issue = [&](int v, int buf, int2 tr) {
+        const int xbv = tr.y >> 16;
         const int l0 = xbv ? r0 : c0;
         const int nlines = min(kTile, (xbv ? H : W) - l0);
         int elo, ne;
@@ -799,8 +798,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             elo = lo;
             ne = (hi - lo + 1) & ~1;
         }
-        const int2 tr = it.trange[(size_t)v * ntiles + tile];
-        const int kb = tr.x, kn = tr.y;
+        const int kb = tr.x, kn = tr.y & 0xFFFF;
         if (lane == 0) {
             krange[4 * buf] = kb;
             krange[4 * buf + 1] = kn;
@@ -826,14 +824,18 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         for (int b = 0; b < kBI; b++) acc[q][b] = 0.0f;
 
     if (warp == 0) {
-        issue(0, 0);
-        if (V > 1) issue(1, 1);
+        issue(0, 0, it.trange[tile]);
+        if (V > 1) issue(1, 1, it.trange[(size_t)ntiles + tile]);
     }
+    // warp w issues the copies of views w + 2, w + 10, ...: it loads each
+    // view's staged range one turn (8 views) ahead
+    int2 tr_next = make_int2(0, 0);
+    if (warp + 2 < V) tr_next = it.trange[(size_t)(warp + 2) * ntiles + tile];
     int vstop = V;   // first view not waited for (the copies of vstop may be in flight)
     for (int v = 0; v < V; v++) {
         const int buf = v % kAdjBufs;
-        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
-        uses[buf]++;
+        if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
+        ph.flip(buf);
         // one barrier per view: past it every warp has finished view v - 1
         __syncthreads();
         if (abort_flag) {
@@ -842,7 +844,11 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         }
         // so the copies of view v + 2 can go into the buffer of view v - 1; the
         // issuing warp rotates so that no warp carries every view's copies
-        if (warp == (v & (kWarps - 1)) && v + 2 < V) issue(v + 2, (v + 2) % kAdjBufs);
+        if (warp == (v & (kWarps - 1)) && v + 2 < V) {
+            const int2 tr = tr_next;
+            if (v + 2 + kWarps < V) tr_next = it.trange[(size_t)(v + 2 + kWarps) * ntiles + tile];
+            issue(v + 2, (v + 2) % kAdjBufs, tr);
+        }
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
         const int xb = krange[4 * buf + 3];
         const int2 *mp = mapb + (size_t)buf * kTile * kMapE;
@@ -908,8 +914,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         // let the copies of view vstop (issued, not waited for) land
         for (int u = vstop; u < V && u < vstop + 1; u++) {
             const int b = u % kAdjBufs;
-            if (tid == 0) dd_mbar_wait(&bar[b], uses[b] & 1);
-            uses[b]++;
+            if (tid == 0) dd_mbar_wait(&bar[b], ph.parity(b));
+            ph.flip(b);
         }
         __syncthreads();
         return false;

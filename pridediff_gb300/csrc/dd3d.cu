@@ -571,14 +571,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
 #pragma unroll
         for (int b = 0; b < kNB; b++) acc[q][b] = 0.0f;
 
-    uint32_t uses[2] = {0u, 0u};
+    DdPhases ph;
     int inflight = -1;
     if (tid == 0) issue(0, 0);
     for (int v = 0; v < a.V; v++) {
         const int buf = v & 1;
         if (tid == 0 && v + 1 < a.V) issue(v + 1, buf ^ 1);
-        if (!dd_mbar_wait(&bar[buf], uses[buf] & 1)) abort_flag = 1;
-        uses[buf]++;
+        if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
+        ph.flip(buf);
         __syncthreads();
         if (abort_flag) {
             inflight = (v + 1 < a.V) ? (buf ^ 1) : -1;
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
         __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
     if (abort_flag) {
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], uses[inflight] & 1);
+        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], ph.parity(inflight));
         if (tid == 0) atomicExch(a.status, DD_ERR_TIMEOUT);
         return;
     }

@@ -50,6 +50,15 @@ __device__ __forceinline__ bool dd_mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
+// Phase parities of a CTA's mbarriers, one bit per barrier.  A bit mask keeps
+// them in a register; an array indexed by the buffer number would live in
+// local memory and put a load and a store in front of every wait.
+struct DdPhases {
+    uint32_t bits = 0;
+    __device__ __forceinline__ uint32_t parity(int b) const { return (bits >> b) & 1u; }
+    __device__ __forceinline__ void flip(int b) { bits ^= 1u << b; }
+};
+
 // Bounded wait for the phase with the given parity.  Returns false on timeout.
 __device__ __forceinline__ bool dd_mbar_wait(uint64_t *bar, uint32_t parity) {
     for (uint32_t it = 0; it < DD_WAIT_LIMIT; ++it) {
