@@ -782,39 +782,59 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     if (tid == 0) abort_flag = 0;
     __syncthreads();
 
-    // one warp: copies of view v into buffer buf (lane i moves line i's entries)
+    // What view v's copies move, from its staged range {first bin, bins | xb << 16}.
+    struct Cp {
+        int xb, l0, nlines, elo, ne, kb, kn;
+    };
     const int tile = (r0 / kTile) * tiles_x(&g) + c0 / kTile, ntiles = tiles_n(&g);
-    auto issue = [&](int v, int buf, int2 tr) {
-        const int xbv = tr.y >> 16;
-        const int l0 = xbv ? r0 : c0;
-        const int nlines = min(kTile, (xbv ? H : W) - l0);
-        int elo, ne;
-        if (xbv) {   // pixels c0 .. c0+31 of rows r0 ..: boundaries c0-1 .. c0+31
-            elo = c0;
-            ne = min(kTile + 2, ms - c0);
-        } else {     // pixels H-r0-32 .. H-r0-1 of columns c0 ..
+    auto desc = [&](int2 tr) {
+        Cp d;
+        d.xb = tr.y >> 16;
+        d.l0 = d.xb ? r0 : c0;
+        d.nlines = min(kTile, (d.xb ? H : W) - d.l0);
+        if (d.xb) {   // pixels c0 .. c0+31 of rows r0 ..: boundaries c0-1 .. c0+31
+            d.elo = c0;
+            d.ne = min(kTile + 2, ms - c0);
+        } else {      // pixels H-r0-32 .. H-r0-1 of columns c0 ..
             const int lo = max(H - r0 - kTile, 0) & ~1;
             const int hi = min(H - r0 + 1, ms);
-            elo = lo;
-            ne = (hi - lo + 1) & ~1;
+            d.elo = lo;
+            d.ne = (hi - lo + 1) & ~1;
         }
-        const int kb = tr.x, kn = tr.y & 0xFFFF;
-        if (lane == 0) {
-            krange[4 * buf] = kb;
-            krange[4 * buf + 1] = kn;
-            krange[4 * buf + 2] = elo;
-            krange[4 * buf + 3] = xbv;
-            dd_mbar_expect_tx(&bar[buf], (uint32_t)((nlines * ne + nb * kn) * (int)sizeof(int2) + kTile * (int)sizeof(float)));
+        d.kb = tr.x;
+        d.kn = tr.y & 0xFFFF;
+        return d;
+    };
+    // thread 0 arms a buffer's barrier with the byte count of its next view,
+    // before any warp issues a copy into it
+    auto arm = [&](int buf, const Cp &d) {
+        dd_mbar_expect_tx(&bar[buf], (uint32_t)((d.nlines * d.ne + nb * d.kn) * (int)sizeof(int2) +
+                                                kTile * (int)sizeof(float)));
+    };
+    // Every warp issues its share of view v's copies, so that no warp carries
+    // a long run of them: lanes 0-3 move the map rows of lines warp + 8 lane,
+    // lane 4 of warp b < nb the detector-table slice of image b, lane 5 of
+    // warp 0 the line scales.
+    auto issue = [&](int v, int buf, const Cp &d) {
+        if (tid == 0) {
+            krange[4 * buf] = d.kb;
+            krange[4 * buf + 1] = d.kn;
+            krange[4 * buf + 2] = d.elo;
+            krange[4 * buf + 3] = d.xb;
         }
-        __syncwarp();
-        if (lane < nlines)
-            dd_bulk_g2s(mapb + ((size_t)buf * kTile + lane) * kMapE, it.amap + ((size_t)v * nl + l0 + lane) * ms + elo,
-                        (uint32_t)(ne * sizeof(int2)), &bar[buf]);
-        if (lane < nb && kn > 0)
-            dd_bulk_g2s(stage + ((size_t)buf * kBI + lane) * kStage, dtab + ((size_t)(b0 + lane) * V + v) * rsd + kb,
-                        (uint32_t)(kn * sizeof(float2)), &bar[buf]);
-        if (lane == 31)
-            dd_bulk_g2s(alb + buf * kTile, it.alpha + (size_t)v * sal + l0, (uint32_t)(kTile * sizeof(float)), &bar[buf]);
+        const int li = warp + kWarps * lane;
+        if (lane < kLinesPerWarp) {
+            if (li < d.nlines)
+                dd_bulk_g2s(mapb + ((size_t)buf * kTile + li) * kMapE,
+                            it.amap + ((size_t)v * nl + d.l0 + li) * ms + d.elo, (uint32_t)(d.ne * sizeof(int2)),
+                            &bar[buf]);
+        } else if (lane == kLinesPerWarp) {
+            if (warp < nb && d.kn > 0)
+                dd_bulk_g2s(stage + ((size_t)buf * kBI + warp) * kStage, dtab + ((size_t)(b0 + warp) * V + v) * rsd + d.kb,
+                            (uint32_t)(d.kn * sizeof(float2)), &bar[buf]);
+        } else if (lane == kLinesPerWarp + 1 && warp == 0) {
+            dd_bulk_g2s(alb + buf * kTile, it.alpha + (size_t)v * sal + d.l0, (uint32_t)(kTile * sizeof(float)), &bar[buf]);
+        }
     };
 
     float acc[kLinesPerWarp][kBI];
@@ -823,17 +843,29 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
 #pragma unroll
         for (int b = 0; b < kBI; b++) acc[q][b] = 0.0f;
 
-    if (warp == 0) {
-        issue(0, 0, it.trange[tile]);
-        if (V > 1) issue(1, 1, it.trange[(size_t)ntiles + tile]);
+    {
+        const Cp d0 = desc(it.trange[tile]);
+        const Cp d1 = desc(V > 1 ? it.trange[(size_t)ntiles + tile] : make_int2(0, 0));
+        if (tid == 0) {
+            arm(0, d0);
+            if (V > 1) arm(1, d1);
+        }
+        __syncthreads();
+        issue(0, 0, d0);
+        if (V > 1) issue(1, 1, d1);
     }
-    // warp w issues the copies of views w + 2, w + 10, ...: it loads each
-    // view's staged range one turn (8 views) ahead
-    int2 tr_next = make_int2(0, 0);
-    if (warp + 2 < V) tr_next = it.trange[(size_t)(warp + 2) * ntiles + tile];
+    int2 tr_next = (V > 2) ? it.trange[(size_t)2 * ntiles + tile] : make_int2(0, 0);   // view v + 2
     int vstop = V;   // first view not waited for (the copies of vstop may be in flight)
     for (int v = 0; v < V; v++) {
         const int buf = v % kAdjBufs;
+        const bool more = v + 2 < V;
+        Cp dn;
+        if (more) {
+            dn = desc(tr_next);
+            // the phase of view v - 1 on this barrier was waited for before the
+            // previous barrier, so it can be armed for view v + 2 now
+            if (tid == 0) arm((v + 2) % kAdjBufs, dn);
+        }
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         // one barrier per view: past it every warp has finished view v - 1
@@ -842,12 +874,10 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             vstop = v + 1;
             break;
         }
-        // so the copies of view v + 2 can go into the buffer of view v - 1; the
-        // issuing warp rotates so that no warp carries every view's copies
-        if (warp == (v & (kWarps - 1)) && v + 2 < V) {
-            const int2 tr = tr_next;
-            if (v + 2 + kWarps < V) tr_next = it.trange[(size_t)(v + 2 + kWarps) * ntiles + tile];
-            issue(v + 2, (v + 2) % kAdjBufs, tr);
+        // so the copies of view v + 2 go into the buffer of view v - 1
+        if (more) {
+            issue(v + 2, (v + 2) % kAdjBufs, dn);
+            if (v + 3 < V) tr_next = it.trange[(size_t)(v + 3) * ntiles + tile];
         }
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
         const int xb = krange[4 * buf + 3];
