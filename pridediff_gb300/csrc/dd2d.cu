@@ -200,41 +200,48 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
-// Adjoint map of fan beams (plan time): for every (view, walked line,
-// boundary index b = -1 .. npix-1) the detector bin k and offset u - d_k of
-// the clamped boundary value u, exactly as the pixel-gather adjoint needs
-// them (k = -1 outside the walk), and the line's DD-BP scale.  Boundary
-// i0 - 1 is the walk start.  One thread per entry.
+// Adjoint map of fan beams (plan time): one CTA per (tile, view) fills the
+// tile's block.  For each of the tile's walked lines and boundary indices
+// b = e - 1 (e from map_first()): the detector bin k and offset u - d_k of the
+// clamped boundary value u, exactly as the pixel-gather adjoint needs them
+// (k = -1 where the walk does not reach b; boundary i0 - 1 is the walk
+// start); then the lines' DD-BP scales.
 template <int GEOM>
 __global__ void __launch_bounds__(128)
-k_amap(dd_geom2d g, int V, int nl, const DdView2 *__restrict__ views, const float *__restrict__ angles,
-       const float *__restrict__ dp, const DdLine *__restrict__ lines, int2 *__restrict__ amap,
-       float *__restrict__ alpha) {
-    const int e = blockIdx.x * 128 + threadIdx.x, line = blockIdx.y, v = blockIdx.z;
+k_amap(dd_geom2d g, int nl, const DdView2 *__restrict__ views, const float *__restrict__ angles,
+       const float *__restrict__ dp, const DdLine *__restrict__ lines, unsigned char *__restrict__ amap) {
+    const int t = blockIdx.x, v = blockIdx.y;
+    const int c0 = (t % tiles_x(&g)) * kTile, r0 = (t / tiles_x(&g)) * kTile;
     const int ms = map_stride(&g), D = g.num_det;
-    if (e >= ms) return;
     const DdView2 vw = views[v];
     const int nline = vw.xb ? g.height : g.width;
-    int2 *out = amap + ((size_t)v * nl + line) * ms + e;
-    if (line >= nline) {
-        *out = make_int2(-1, 0);
-        if (e == 0) alpha[(size_t)v * alpha_stride(nl) + line] = 0.0f;
-        return;
-    }
-    const DdLine &L = lines[(size_t)v * nl + line];
-    if (e == 0) alpha[(size_t)v * alpha_stride(nl) + line] = L.h.alpha;
-    const int b = e - 1, i0 = L.h.i0, nend = L.h.nend;
-    if (L.h.npiece == 0 || b < i0 - 1 || b >= nend) {
-        *out = make_int2(-1, 0);
-        return;
-    }
-    const float bound0 = L.h.bound0;
+    const int l0 = vw.xb ? r0 : c0, elo = map_first(&g, vw.xb, c0, r0);
+    int2 *ent = reinterpret_cast<int2 *>(amap + ((size_t)v * tiles_n(&g) + t) * kMapBlkBytes);
+    float *alpha = reinterpret_cast<float *>(ent + kTile * kMapE);
     const float *dpv = dp + (size_t)v * (D + 1);
-    const float u = (b == i0 - 1) ? bound0 : dd_boundary(&L, b, L.p[0].Q + (float)(b - L.p[0].gb) * L.p[0].dl);
-    const float uu = fminf(fmaxf(u, bound0), dpv[D]);
-    float dk;
-    const int k = fan_bin(GEOM, g, vw, angles[v], dpv, uu, L.h.idet0, &dk);
-    *out = make_int2(k, __float_as_int(uu - dk));
+    const float ang = angles[v];
+    for (int i = threadIdx.x; i < kTile * kMapE; i += 128) {
+        const int li = i / kMapE, e = elo + (i - li * kMapE), line = l0 + li;
+        int2 val = make_int2(-1, 0);
+        if (line < nline && e < ms) {
+            const DdLine &L = lines[(size_t)v * nl + line];
+            const int b = e - 1, i0 = L.h.i0, nend = L.h.nend;
+            if (L.h.npiece > 0 && b >= i0 - 1 && b < nend) {
+                const float bound0 = L.h.bound0;
+                const float u =
+                    (b == i0 - 1) ? bound0 : dd_boundary(&L, b, L.p[0].Q + (float)(b - L.p[0].gb) * L.p[0].dl);
+                const float uu = fminf(fmaxf(u, bound0), dpv[D]);
+                float dk;
+                const int k = fan_bin(GEOM, g, vw, ang, dpv, uu, L.h.idet0, &dk);
+                val = make_int2(k, __float_as_int(uu - dk));
+            }
+        }
+        ent[i] = val;
+    }
+    if (threadIdx.x < kTile) {
+        const int line = l0 + threadIdx.x;
+        alpha[threadIdx.x] = line < nline ? lines[(size_t)v * nl + line].h.alpha : 0.0f;
+    }
 }
 
 // Detector-table slice staged per (view, 32x32 tile) by the fan-beam adjoint
@@ -265,8 +272,8 @@ template <int GEOM, int OPK>
 __global__ void __launch_bounds__(kThreads)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const DdView2 *__restrict__ views, const float *__restrict__ dp,
-      const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines, const int2 *__restrict__ amap,
-      const float *__restrict__ alpha, const int2 *__restrict__ trange, const float2 *__restrict__ dtab,
+      const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines, const unsigned char *__restrict__ amap,
+      const int2 *__restrict__ trange, const float2 *__restrict__ dtab,
       float *__restrict__ out,
       const float *__restrict__ base, float scale, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -286,7 +293,6 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     it.lines = lines;
     it.dlines = dlines;
     it.amap = amap;
-    it.alpha = alpha;
     it.trange = trange;
     it.dtab = dtab;
     it.out = out;
@@ -380,17 +386,16 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
     k_lines<<<gl, 64, 0, st>>>(geom, *g, angles, V, P.nl, views, dp, lines, dlines);
     int n = 2;
     if (geom != DD_GEOM_PARA && with_map) {
-        const dim3 gm((unsigned)((map_stride(g) + 127) / 128), (unsigned)P.nl, (unsigned)V);
+        const dim3 gm((unsigned)tiles_n(g), (unsigned)V);
         const float *ang = (const float *)(base + P.ang);
-        int2 *amap = (int2 *)(base + P.amap);
-        float *alpha = (float *)(base + P.alpha);
+        unsigned char *amap = (unsigned char *)(base + P.amap);
         int2 *trange = (int2 *)(base + P.trange);
         const int nt = (V * tiles_n(g) + 127) / 128;
         if (geom == DD_GEOM_FLAT) {
-            k_amap<DD_GEOM_FLAT><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+            k_amap<DD_GEOM_FLAT><<<gm, 128, 0, st>>>(*g, P.nl, views, ang, dp, lines, amap);
             k_trange<DD_GEOM_FLAT><<<nt, 128, 0, st>>>(*g, V, views, ang, trange);
         } else {
-            k_amap<DD_GEOM_ARC><<<gm, 128, 0, st>>>(*g, V, P.nl, views, ang, dp, lines, amap, alpha);
+            k_amap<DD_GEOM_ARC><<<gm, 128, 0, st>>>(*g, P.nl, views, ang, dp, lines, amap);
             k_trange<DD_GEOM_ARC><<<nt, 128, 0, st>>>(*g, V, views, ang, trange);
         }
         n += 2;
@@ -441,15 +446,14 @@ static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const float *dp = (const float *)(planb + P.dp);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    const int2 *amap = GEOM == DD_GEOM_PARA ? nullptr : (const int2 *)(planb + P.amap);
-    const float *alpha = GEOM == DD_GEOM_PARA ? nullptr : (const float *)(planb + P.alpha);
+    const unsigned char *amap = GEOM == DD_GEOM_PARA ? nullptr : (const unsigned char *)(planb + P.amap);
     const int2 *trange = GEOM == DD_GEOM_PARA ? nullptr : (const int2 *)(planb + P.trange);
     const AdjSmem S = adj_smem(GEOM);
     auto kern = (op == DD_OP_PROJ_T) ? k_adj<GEOM, 0> : (op == DD_OP_BPROJ) ? k_adj<GEOM, 1> : k_adj<GEOM, 2>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
-    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, amap, alpha, trange,
+    kern<<<grid, kThreads, S.total, st>>>(*g, B, V, P.nl, angles, views, dp, lines, dlines, amap, trange,
                                           dtab, out, base, scale, status);
     prof_end(pr, st);
     g_launches++;

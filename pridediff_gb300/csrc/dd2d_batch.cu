@@ -33,7 +33,7 @@ struct BatchInst {
     long long img_off, sino_off;   // elements: packed images / sinograms
     long long tabx_off, taby_off;  // float2: forward tables in the workspace
     long long dtab_off;            // float2: adjoint tables in the workspace
-    long long views, ang, dp, bcoef, lines, dlines, amap, alpha, trange;   // PlanLayout offsets
+    long long views, ang, dp, bcoef, lines, dlines, amap, trange;   // PlanLayout offsets
 };
 
 struct BatchLayout {
@@ -68,7 +68,6 @@ static BatchLayout batch_layout(int scan, const dd_instance2d *in, int n, int bi
         d.lines = (long long)P.lines;
         d.dlines = (long long)P.dlines;
         d.amap = (long long)P.amap;
-        d.alpha = (long long)P.alpha;
         d.trange = (long long)P.trange;
         const int W = d.g.width, H = d.g.height, D = d.g.num_det;
         d.img_off = img;
@@ -267,8 +266,7 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
         it.dp = reinterpret_cast<const float *>(pb + d.dp);
         it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
         it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
-        it.amap = reinterpret_cast<const int2 *>(pb + d.amap);
-        it.alpha = reinterpret_cast<const float *>(pb + d.alpha);
+        it.amap = reinterpret_cast<const unsigned char *>(pb + d.amap);
         it.trange = reinterpret_cast<const int2 *>(pb + d.trange);
         it.dtab = dtabs + d.dtab_off;
         it.out = out + d.img_off;

@@ -18,6 +18,13 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kBinsPerWarp = 31;   // 32 boundaries -> 31 bins per warp pass
 constexpr int kBI = 4;             // images per CTA (geometry amortised over them)
+constexpr int kTile = 32;          // adjoint work item: 32 x 32 pixels
+// Adjoint-map entries per walked line of a tile: the boundaries of a 32-pixel
+// run plus one below it, from an even first entry.
+constexpr int kMapE = 36;
+// One adjoint-map block (a view, a tile): kTile rows of kMapE entries {bin,
+// offset}, then the kTile lines' DD-BP scales; one bulk copy moves it.
+constexpr int kMapBlkBytes = kTile * kMapE * 8 + kTile * 4;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n+1 float2, 16-B rows
@@ -26,20 +33,29 @@ __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n
 // Workspace layout
 // ---------------------------------------------------------------------------
 struct PlanLayout {
-    size_t views, ang, dp, bcoef, lines, dlines, amap, alpha, trange, total;
+    size_t views, ang, dp, bcoef, lines, dlines, amap, trange, total;
     int nl;   // line records per view = max(H, W)
 };
 
-// Adjoint map of fan beams: per (view, walked line) a row of map_stride()
-// entries {bin k, offset} for the boundary indices -1 .. npix-1 (entry e holds
-// boundary e - 1); alpha_stride() per-line DD-BP scales per view.
+// Adjoint map of fan beams, one block per (view, tile) in tile-major order.
+// Entry e of a walked line holds its boundary e - 1 (e in 0 .. map_stride()-1
+// over the line); a block keeps, for each of the tile's kTile walked lines,
+// the kMapE entries from the tile's first entry (map_first()).
 __host__ __device__ inline int map_stride(const dd_geom2d *g) {
     return rs_entries(g->width > g->height ? g->width : g->height);
 }
-__host__ __device__ inline int alpha_stride(int nl) { return (nl + 31) & ~31; }
 // 32 x 32 tiles of the image (the adjoint's work items); tile = ty * ntx + tx
 __host__ __device__ inline int tiles_x(const dd_geom2d *g) { return (g->width + 31) / 32; }
 __host__ __device__ inline int tiles_n(const dd_geom2d *g) { return tiles_x(g) * ((g->height + 31) / 32); }
+// First map entry a tile's block keeps.  Rows (xb views): pixels c0 .. c0+31
+// have boundaries c0-1 .. c0+31, entries c0 .. c0+32.  Columns: pixels
+// H-r0-32 .. H-r0-1 along the column, entries from an even index at or below
+// H-r0-32 (so that 36 entries always reach H-r0).
+__host__ __device__ inline int map_first(const dd_geom2d *g, int xb, int c0, int r0) {
+    if (xb) return c0;
+    const int lo = g->height - r0 - kTile;
+    return (lo > 0 ? lo : 0) & ~1;
+}
 
 // with_map = false leaves out the adjoint map (plans that only serve the
 // forward-type operators, e.g. one-shot forward calls); every other offset is
@@ -56,10 +72,9 @@ inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V, bool with_map
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
     L.dlines = o;
     if (scan == DD_SCAN_PARA) o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
-    L.amap = L.alpha = L.trange = o;
+    L.amap = L.trange = o;
     if (scan != DD_SCAN_PARA && with_map) {
-        L.amap = o; o = align_up(o + sizeof(int2) * (size_t)V * L.nl * map_stride(g), 256);
-        L.alpha = o; o = align_up(o + sizeof(float) * (size_t)V * alpha_stride(L.nl), 256);
+        L.amap = o; o = align_up(o + (size_t)kMapBlkBytes * V * tiles_n(g), 256);
         L.trange = o; o = align_up(o + sizeof(int2) * (size_t)V * tiles_n(g), 256);
     }
     L.total = o;
@@ -378,7 +393,6 @@ __device__ __forceinline__ void init_bars(uint64_t *bar, int n = 2) {
 // registers (row-major ownership for x-branch views, column-major for
 // y-branch views, merged through shared memory at the end).
 // ---------------------------------------------------------------------------
-constexpr int kTile = 32;
 constexpr int kLinesPerWarp = kTile / kWarps;   // 4
 
 // Fan: integral of the detector function up to u (clamped) for image b.
@@ -411,9 +425,6 @@ __device__ __forceinline__ void det_index_fan(int geom, const dd_geom2d &g, cons
 // gather from global memory instead.
 constexpr int kStage = 256;
 
-// Staged adjoint-map entries per line and view: the boundaries of a 32-pixel
-// run plus one below it, from an even first entry.
-constexpr int kMapE = 36;
 // Views in flight in the fan-beam adjoint: the copies of view v + 2 are issued
 // while view v is computed (part of the map comes from HBM).
 constexpr int kAdjBufs = 3;
@@ -423,18 +434,17 @@ constexpr int kAdjBufs = 3;
 // table slices and per-line scales.
 struct AdjSmem {
     int rec, drec, kd, stage, krange, bar, total;
-    int map, alpha;
+    int map;
 };
 
 __host__ __device__ inline AdjSmem adj_smem(int geom) {
     AdjSmem s;
     int o = 0;
-    s.map = s.alpha = 0;
+    s.map = 0;
     if (geom != DD_GEOM_PARA) {
         s.rec = s.drec = s.kd = 0;
-        s.map = o; o += kAdjBufs * kTile * kMapE * (int)sizeof(int2);
+        s.map = o; o += kAdjBufs * kMapBlkBytes;
         s.stage = o; o += kAdjBufs * kBI * kStage * (int)sizeof(float2);
-        s.alpha = o; o += kAdjBufs * kTile * (int)sizeof(float);
         s.krange = o; o += 4 * kAdjBufs * (int)sizeof(int);
         s.bar = o; o += kAdjBufs * (int)sizeof(uint64_t);
         s.total = (o + 127) & ~127;
@@ -511,8 +521,7 @@ struct AdjItem {
     const DdView2 *views;
     const float *dp;
     const DdLine *lines, *dlines;
-    const int2 *amap;            // fan beams: adjoint map (plan)
-    const float *alpha;          // fan beams: per-line DD-BP scales (plan)
+    const unsigned char *amap;   // fan beams: adjoint-map blocks (plan)
     const int2 *trange;          // fan beams, per (view, tile): {first staged bin, bins | xb << 16} (plan)
     const float2 *dtab;          // detector tables of image 0 of the instance
     float *out;                  // image 0 of the instance
@@ -769,10 +778,9 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     const AdjSmem SL = adj_smem(GEOM);
     const int V = it.V, nl = it.nl;
     const int W = g.width, H = g.height, D = g.num_det;
-    const int rsd = rs_entries(D), ms = map_stride(&g), sal = alpha_stride(nl);
-    int2 *mapb = reinterpret_cast<int2 *>(smem + SL.map);          // [2][kTile][kMapE]
-    float2 *stage = reinterpret_cast<float2 *>(smem + SL.stage);   // [2][kBI][kStage]
-    float *alb = reinterpret_cast<float *>(smem + SL.alpha);       // [2][kTile]
+    const int rsd = rs_entries(D);
+    unsigned char *mapb = smem + SL.map;                           // [kAdjBufs] map blocks
+    float2 *stage = reinterpret_cast<float2 *>(smem + SL.stage);   // [kAdjBufs][kBI][kStage]
     int *krange = reinterpret_cast<int *>(smem + SL.krange);       // per buffer: first bin, bins, first entry
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SL.bar);
     __shared__ int abort_flag;
@@ -784,23 +792,13 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
 
     // What view v's copies move, from its staged range {first bin, bins | xb << 16}.
     struct Cp {
-        int xb, l0, nlines, elo, ne, kb, kn;
+        int xb, elo, kb, kn;
     };
     const int tile = (r0 / kTile) * tiles_x(&g) + c0 / kTile, ntiles = tiles_n(&g);
     auto desc = [&](int2 tr) {
         Cp d;
         d.xb = tr.y >> 16;
-        d.l0 = d.xb ? r0 : c0;
-        d.nlines = min(kTile, (d.xb ? H : W) - d.l0);
-        if (d.xb) {   // pixels c0 .. c0+31 of rows r0 ..: boundaries c0-1 .. c0+31
-            d.elo = c0;
-            d.ne = min(kTile + 2, ms - c0);
-        } else {      // pixels H-r0-32 .. H-r0-1 of columns c0 ..
-            const int lo = max(H - r0 - kTile, 0) & ~1;
-            const int hi = min(H - r0 + 1, ms);
-            d.elo = lo;
-            d.ne = (hi - lo + 1) & ~1;
-        }
+        d.elo = map_first(&g, d.xb, c0, r0);
         d.kb = tr.x;
         d.kn = tr.y & 0xFFFF;
         return d;
@@ -808,13 +806,10 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     // thread 0 arms a buffer's barrier with the byte count of its next view,
     // before any warp issues a copy into it
     auto arm = [&](int buf, const Cp &d) {
-        dd_mbar_expect_tx(&bar[buf], (uint32_t)((d.nlines * d.ne + nb * d.kn) * (int)sizeof(int2) +
-                                                kTile * (int)sizeof(float)));
+        dd_mbar_expect_tx(&bar[buf], (uint32_t)(kMapBlkBytes + nb * d.kn * (int)sizeof(float2)));
     };
-    // Every warp issues its share of view v's copies, so that no warp carries
-    // a long run of them: lanes 0-3 move the map rows of lines warp + 8 lane,
-    // lane 4 of warp b < nb the detector-table slice of image b, lane 5 of
-    // warp 0 the line scales.
+    // View v's copies, one per warp: warp 0 moves the tile's map block, warp
+    // b + 1 (b < nb) the detector-table slice of image b.
     auto issue = [&](int v, int buf, const Cp &d) {
         if (tid == 0) {
             krange[4 * buf] = d.kb;
@@ -822,18 +817,14 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             krange[4 * buf + 2] = d.elo;
             krange[4 * buf + 3] = d.xb;
         }
-        const int li = warp + kWarps * lane;
-        if (lane < kLinesPerWarp) {
-            if (li < d.nlines)
-                dd_bulk_g2s(mapb + ((size_t)buf * kTile + li) * kMapE,
-                            it.amap + ((size_t)v * nl + d.l0 + li) * ms + d.elo, (uint32_t)(d.ne * sizeof(int2)),
+        if (lane == 0) {
+            if (warp == 0)
+                dd_bulk_g2s(mapb + (size_t)buf * kMapBlkBytes, it.amap + ((size_t)v * ntiles + tile) * kMapBlkBytes,
+                            (uint32_t)kMapBlkBytes, &bar[buf]);
+            else if (warp <= nb && d.kn > 0)
+                dd_bulk_g2s(stage + ((size_t)buf * kBI + warp - 1) * kStage,
+                            dtab + ((size_t)(b0 + warp - 1) * V + v) * rsd + d.kb, (uint32_t)(d.kn * sizeof(float2)),
                             &bar[buf]);
-        } else if (lane == kLinesPerWarp) {
-            if (warp < nb && d.kn > 0)
-                dd_bulk_g2s(stage + ((size_t)buf * kBI + warp) * kStage, dtab + ((size_t)(b0 + warp) * V + v) * rsd + d.kb,
-                            (uint32_t)(d.kn * sizeof(float2)), &bar[buf]);
-        } else if (lane == kLinesPerWarp + 1 && warp == 0) {
-            dd_bulk_g2s(alb + buf * kTile, it.alpha + (size_t)v * sal + d.l0, (uint32_t)(kTile * sizeof(float)), &bar[buf]);
         }
     };
 
@@ -881,7 +872,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         }
         const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
         const int xb = krange[4 * buf + 3];
-        const int2 *mp = mapb + (size_t)buf * kTile * kMapE;
+        const int2 *mp = reinterpret_cast<const int2 *>(mapb + (size_t)buf * kMapBlkBytes);
+        const float *alb = reinterpret_cast<const float *>(mp + kTile * kMapE);   // line scales
         const float2 *sb = stage + (size_t)buf * kBI * kStage;
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) {
@@ -897,7 +889,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             }
             const int2 up = mp[lr * kMapE + eu], low = mp[lr * kMapE + eu - 1];
             if (up.x < 0 || low.x < 0) continue;
-            float wgt = (OPK == 0) ? 1.0f : alb[buf * kTile + lr];
+            float wgt = (OPK == 0) ? 1.0f : alb[lr];
             if (OPK == 2) {
                 const DdView2 vw = it.views[v];
                 const int line = xb ? r : c, pi = xb ? c : H - 1 - r;
