@@ -160,7 +160,7 @@ __host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi =
     s.rec = o; o += 2 * (int)sizeof(DdLine);
     s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * (int)sizeof(DdLine);
     s.tab = o; o += 2 * bi * rsmax * (int)sizeof(float2);
-    s.kt = o; o += bi * 32 * (int)sizeof(float) * 2;   // K for pixel pieces (x2 for para det)
+    s.kt = o; o += bi * 32 * (int)sizeof(float);   // K of the pixel pieces
     s.dp = o; o += ((D + 1 + 3) & ~3) * (int)sizeof(float);
     s.bar = o; o += 2 * (int)sizeof(uint64_t);
     s.total = (o + 127) & ~127;
