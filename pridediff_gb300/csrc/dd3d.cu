@@ -249,7 +249,7 @@ struct Fwd3Args {
 // warp, in rotation, one line ahead -- into shared memory, and reused by all
 // 64 rows.  Line records arrive by bulk copies (TMA) two lines ahead.
 template <int GEOM, int FAMILY>
-__global__ void __launch_bounds__(kThreads, 2) k_fwd3(const Fwd3Args a) {
+__global__ void __launch_bounds__(kThreads, 3) k_fwd3(const Fwd3Args a) {
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
     const int v = blockIdx.x, cg = blockIdx.y;
@@ -510,7 +510,7 @@ __device__ __forceinline__ bool slab_visible(const dd_geom3d &g, const DdView3 &
 // (x, y) voxel column of a 16 x 16 tile.  Views whose detector cannot see the
 // slab are skipped when their copy would be issued.
 template <int GEOM, int FAMILY>
-__global__ void __launch_bounds__(kThreads, 2) k_adj3(const Adj3Args a) {
+__global__ void __launch_bounds__(kThreads, 3) k_adj3(const Adj3Args a) {
     extern __shared__ __align__(128) unsigned char sm[];
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
