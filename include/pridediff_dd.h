@@ -201,6 +201,17 @@ int dd2d_sysmatrix_count(int scan, const dd_geom2d *g, const void *plan, int num
 int dd2d_sysmatrix_fill(int scan, const dd_geom2d *g, const void *plan, int num_view, const long long *offsets,
                         long long *rows, long long *cols, float *vals, dd_stream_t stream);
 
+/* ---- FBP filtering ---------------------------------------------------------
+ * Replaces `nn.functional.conv2d(sino * weight, filter, padding=(0, D - 1))`
+ * (conv3d for the 3-D geometries) in deeprecon's filtered_backprojection
+ * (deeprecon/torch/projector/projector.py:192-213, 368-390, 554-563): for
+ * `rows` detector rows of num_det bins,
+ *   out[i][k] = sum_n taps[n - k + num_det - 1] * (weight[i % wrows][n] * in[i][n]),
+ * taps holding 2 num_det - 1 entries (filter.py:8-30 builds them).  weight
+ * may be NULL (unit weight).  Device pointers; out must not alias in. */
+int dd_fbp_filter(const float *in, float *out, const float *weight, int wrows, const float *taps,
+                  long long rows, int num_det, dd_stream_t stream);
+
 /* ---- 3-D: cone-flat, cone-arc, spiral --------------------------------------
  * Same conventions as 2-D.  source_pos is the spiral source table (4, V) on
  * the device (RadonTorch.cpp:1040-1043); pass NULL for the cone geometries.
@@ -266,7 +277,7 @@ int dd_ProjFanFlatDis2d_noalloc(const dd_geom2d *g, const float *in, float *out,
 /* ---- diagnostics ----------------------------------------------------------
  * No counterpart in the reference (it has no instrumentation).  Kernel kinds
  * for dd_profile_read: */
-enum { DD_KERNEL_FORWARD = 0, DD_KERNEL_ADJOINT = 1, DD_KERNEL_TABLES = 2, DD_KERNEL_PLAN = 3 };
+enum { DD_KERNEL_FORWARD = 0, DD_KERNEL_ADJOINT = 1, DD_KERNEL_TABLES = 2, DD_KERNEL_PLAN = 3, DD_KERNEL_FILTER = 4 };
 /* Number of kernels this library has launched in the process. */
 unsigned long long dd_launch_count(void);
 /* Record CUDA events around every subsequent launch (and reset the records);

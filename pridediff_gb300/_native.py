@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_BUILD, "libpridediff_dd.so")
 INCLUDE = os.path.join(_ROOT, "include")
 
 # translation units of the library (compiled in parallel)
-SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd2d_sysmat.cu", "dd3d.cu", "dd2d_noalloc.cu"]
+SOURCES = ["dd2d.cu", "dd2d_batch.cu", "dd2d_sysmat.cu", "dd3d.cu", "dd2d_noalloc.cu", "dd_fbp.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -183,6 +183,8 @@ def _declare(lib):
     lib.dd_status_string.argtypes = [i]
     lib.dd_version.restype = cp
     lib.dd_version.argtypes = []
+    lib.dd_fbp_filter.restype = i
+    lib.dd_fbp_filter.argtypes = [vp, vp, vp, i, vp, ctypes.c_longlong, i, vp]
 
 
 def load():

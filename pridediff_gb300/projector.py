@@ -22,6 +22,7 @@ import torch
 import torch.nn as nn
 from torch import Tensor
 
+from . import fbp
 from . import function as F
 from .filter import filter_generate
 
@@ -162,8 +163,10 @@ class projector2d(nn.Module):
             taps = self.filter
         else:
             taps = self.filter_generate(filter_type.lower(), dtype=sino.dtype).to(sino.device)
-        sino = sino * self.weight
-        filtered = nn.functional.conv2d(sino, taps, padding=(0, self.num_det - 1))
+        if fbp.fused_ok(sino, self.weight, taps):
+            filtered = fbp.weighted_filter(sino, self.weight, taps)
+        else:   # a trainable weight or filter: autograd through the torch convolution
+            filtered = nn.functional.conv2d(sino * self.weight, taps, padding=(0, self.num_det - 1))
         recon = self.backprojection_w(filtered, angles)
         recon = recon * (angles[-1] - angles[0]).abs() / (angles.size(0) - 1)
         if redundant:
@@ -282,8 +285,10 @@ class projector3d(nn.Module):
             taps = self.filter
         else:
             taps = self.filter_generate(filter_type.lower(), dtype=sino.dtype).to(sino.device)
-        sino = sino * self.weight
-        filtered = nn.functional.conv3d(sino, taps, padding=(0, 0, self.num_det[0] - 1))
+        if fbp.fused_ok(sino, self.weight, taps):
+            filtered = fbp.weighted_filter(sino, self.weight, taps)
+        else:   # a trainable weight or filter: autograd through the torch convolution
+            filtered = nn.functional.conv3d(sino * self.weight, taps, padding=(0, 0, self.num_det[0] - 1))
         recon = self.backprojection_w(filtered, angles)
         recon = recon * (angles[-1] - angles[0]).abs() / (angles.size(0) - 1)
         if redundant:
@@ -379,7 +384,9 @@ class projectorsp(nn.Module):
             taps = self.filter
         else:
             taps = self.filter_generate(filter_type.lower(), dtype=sino.dtype).to(sino.device)
-        sino = sino * self.weight
-        filtered = nn.functional.conv3d(sino, taps, padding=(0, 0, self.num_det[0] - 1))
+        if fbp.fused_ok(sino, self.weight, taps):
+            filtered = fbp.weighted_filter(sino, self.weight, taps)
+        else:   # a trainable weight or filter: autograd through the torch convolution
+            filtered = nn.functional.conv3d(sino * self.weight, taps, padding=(0, 0, self.num_det[0] - 1))
         recon = self.backprojection_w(filtered, angles, source_pos)
         return recon * abs(angles[1] - angles[0]) / 2

@@ -5,6 +5,7 @@ oracle/_ref/libddref.so by `make -C oracle`):
 
     python tests/golden/make_golden.py               # operator outputs -> dd2d_golden.npz
     python tests/golden/make_golden.py --sysmatrix   # system matrices  -> sysmat_golden.npz
+    python tests/golden/make_golden.py --fbp         # FBP              -> fbp_golden.npz
 
 Every case stores its seeded inputs and the reference outputs (computed by
 the unmodified deeprecon CPU projectors, single-threaded), so the tests can
@@ -114,8 +115,94 @@ def main_sysmatrix():
     print("wrote", path, os.path.getsize(path) // 1024, "KB")
 
 
+# (name, geometry, projector2d arguments, angles, filter_type, redundant)
+FBP_CASES = [
+    ("flat_fbp", "flat", dict(image_size=(64, 48), num_det=80, pix_size=(0.9, 0.8), det_size=1.3,
+                              iso_source=595.0, source_detector=1085.6, pixshift=(0.5, -0.4), binshift=0.6),
+     np.arange(120) * 2 * np.pi / 120, "ramp", True),
+    ("arc_fbp", "arc", dict(image_size=(64, 48), num_det=80, pix_size=(0.9, 0.8), det_size=1.3,
+                            iso_source=595.0, source_detector=1085.6, pixshift=(0.5, -0.4), binshift=0.6),
+     np.arange(120) * 2 * np.pi / 120, "sheeplogan", True),
+    ("para_fbp", "para", dict(image_size=(64, 48), num_det=95, pix_size=(1.0, 1.1), det_size=1.0,
+                              iso_source=500.0, source_detector=1000.0, pixshift=(0.3, -0.2), binshift=0.25),
+     np.arange(90) * np.pi / 90, "ramp", False),
+]
+
+
+def _reference_projector_module():
+    """deeprecon's own deeprecon.torch.projector package, imported from the
+    reference sources with its compiled `radontorch` extension answered by the
+    reference's CPU projectors (oracle/_ref/libddref.so): the Python code that
+    runs -- weights, filters, the convolution, the scaling -- is the
+    reference's, unmodified."""
+    import importlib.util
+    import types
+
+    import torch
+    stub = types.ModuleType("radontorch")
+    ops = {"Proj": "proj", "ProjTrans": "proj_t", "BackProj": "bproj", "BackProjTrans": "bproj_t",
+           "BackProjWeighted": "bproj_w", "BackProjTransWeighted": "bproj_tw"}
+    geoms = {"Para": "para", "FanFlat": "flat", "FanArc": "arc"}
+
+    def make(geom, op):
+        def f(x, options, angles):
+            y = oracle.ref2d(geom, op, x.detach().cpu().numpy()[:, 0], angles.detach().cpu().numpy(),
+                             options.detach().cpu().numpy())
+            return torch.from_numpy(np.ascontiguousarray(y, dtype=np.float32))[:, None]
+        return f
+
+    for on, o in ops.items():
+        for gn, g in geoms.items():
+            setattr(stub, f"{on}{gn}Dis2d", make(g, o))
+    sys.modules["radontorch"] = stub
+    ref = os.environ.get("REF", "/root/reference/deeprecon")
+    pkg = os.path.join(ref, "deeprecon", "torch", "projector")
+    spec = importlib.util.spec_from_file_location("ref_projector", os.path.join(pkg, "__init__.py"),
+                                                  submodule_search_locations=[pkg])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["ref_projector"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def main_fbp():
+    """deeprecon's projector2d.filtered_backprojection, its filter taps and
+    cosine weights."""
+    import torch
+    if not oracle.have_ref():
+        oracle.build()
+    if not oracle.have_ref():
+        raise SystemExit("reference sources not present: cannot regenerate golden vectors")
+    refp = _reference_projector_module()
+    out = {}
+    for seed, (name, geom, kw, ang, ftype, redundant) in enumerate(FBP_CASES):
+        rng = np.random.default_rng(2000 + seed)
+        ang = np.asarray(ang, np.float32)
+        prj = refp.projector2d(scan_type=geom, filter_type=ftype, **kw)
+        W, H = kw["image_size"]
+        img = ellipse_phantom(H, W, 6, rng)[None]
+        x = torch.from_numpy(img)[:, None]
+        sino = prj.projection(x, torch.from_numpy(ang))
+        rec = prj.filtered_backprojection(sino, torch.from_numpy(ang), redundant=redundant)
+        out[f"{name}/options"] = prj.options.detach().numpy()
+        out[f"{name}/ctor"] = np.asarray([W, H, kw["num_det"], *kw["pix_size"], kw["det_size"], kw["iso_source"],
+                                          kw["source_detector"], *kw["pixshift"], kw["binshift"]], np.float64)
+        out[f"{name}/angles"] = ang
+        out[f"{name}/sino"] = sino.numpy()[:, 0]
+        out[f"{name}/filter"] = prj.filter.detach().numpy().reshape(-1)
+        out[f"{name}/weight"] = prj.weight.detach().numpy()
+        out[f"{name}/fbp"] = rec.numpy()[:, 0]
+        for other in ("ramp", "sheeplogan"):
+            out[f"{name}/taps_{other}"] = prj.filter_generate(other).detach().numpy().reshape(-1)
+    path = os.path.join(HERE, "fbp_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path) // 1024, "KB")
+
+
 if __name__ == "__main__":
     if "--sysmatrix" in sys.argv[1:]:
         main_sysmatrix()
+    elif "--fbp" in sys.argv[1:]:
+        main_fbp()
     else:
         main()
