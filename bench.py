@@ -251,6 +251,40 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
     except Exception as e:   # report, never hide the headline line
         out["plain_per_slice"] = {"error": repr(e)}
 
+    # FBP (deeprecon's filtered_backprojection) of the headline sinograms
+    try:
+        ct = P._native.ctypes
+        proj = P.projector2d(512, 736, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").to(dev)
+        V = y.shape[2]
+        ang = torch.arange(V, dtype=torch.float32, device=dev) * (2 * np.pi / V)
+        with torch.no_grad():
+            fbp = lambda: proj.filtered_backprojection(y, ang)   # noqa: E731
+
+            def composed():   # the reference's composition: torch conv2d, then the weighted BP
+                f = torch.nn.functional.conv2d(y * proj.weight, proj.filter, padding=(0, 735))
+                return proj.backprojection_w(f, ang) * (ang[-1] - ang[0]).abs() / (V - 1) / 2
+
+            ms = _timed(fbp, 3, flush, ev)
+            ms_conv = _timed(composed, 3, flush, ev)
+            lib = P._native.load()
+            lib.dd_profile_enable(1)
+            for _ in range(3):
+                fbp()
+            torch.cuda.synchronize()
+            tot, cnt = ct.c_double(), ct.c_int()
+            lib.dd_profile_read(4, ct.byref(tot), ct.byref(cnt))
+            lib.dd_profile_enable(0)
+        fms = tot.value / max(cnt.value, 1)
+        flops = 2.0 * B * V * 736 * 736
+        out["fbp_16x512_720v"] = {
+            "what": "projector2d.filtered_backprojection of the 16 headline sinograms (cosine weight + ramp "
+                    "filter fused in one kernel, then the weighted DD back-projection, exact-adjoint family)",
+            "ms_per_call": ms, "value": B / (ms / 1e3), "unit": "FBP/s",
+            "ms_per_call_torch_conv2d_composition": ms_conv,
+            "filter_kernel_ms": fms, "filter_kernel_TFLOPs_fp32": flops / (fms / 1e3) / 1e12}
+    except Exception as e:
+        out["fbp_16x512_720v"] = {"error": repr(e)}
+
     # batched uneven DC loop: 24 instances, 50 graph-captured steps, eta 1e-3
     try:
         from pridediff_gb300.batch import UnevenBatch2d

@@ -177,7 +177,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, kFwdImages);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, kFwdImages, WEIGHTED != 0);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     DdPhases ph;
@@ -410,7 +410,7 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
                       int V, const float2 *tx, const float2 *ty, float *out, const float *sub,
                       int *status, cudaStream_t st) {
     const int rsmax = rs_entries(g->width > g->height ? g->width : g->height);
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages);
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, op == DD_OP_BPROJ_TW);
     dim3 grid(V, (B + kFwdImages - 1) / kFwdImages);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);

@@ -129,6 +129,13 @@ __device__ __forceinline__ float piece_K(const DdLine &L, const float2 *tab, int
     return term;
 }
 
+// FBP-weight pixel centre a * pitch + shift, a an exact half-integer offset:
+// one FMA rounds the exact value once.  The reference evaluates the same
+// expression in FP64 and rounds that to FP32, which gives the same float
+// unless the exact value lies within 2^-53 (relative) of an FP32 rounding
+// boundary -- and FP64 arithmetic runs at a small fraction of the FP32 rate.
+__device__ __forceinline__ float pix_centre(float a, float pitch, float shift) { return fmaf(a, pitch, shift); }
+
 struct Loc {
     int p, j;
     float dl, r;
@@ -151,10 +158,11 @@ __device__ __forceinline__ Loc locate(const DdLine &L, float u) {
 // ---------------------------------------------------------------------------
 struct FwdSmem {
     // dynamic layout offsets (bytes)
-    int rec, drec, tab, kt, dp, bar, total;
+    int rec, drec, tab, kt, dp, ws, bar, total;
 };
 
-__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI) {
+// weighted: BackProjTransWeighted also keeps the FBP weights of a line's pixels.
+__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI, bool weighted = false) {
     FwdSmem s;
     int o = 0;
     s.rec = o; o += 2 * (int)sizeof(DdLine);
@@ -162,6 +170,7 @@ __host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi =
     s.tab = o; o += 2 * bi * rsmax * (int)sizeof(float2);
     s.kt = o; o += bi * 32 * (int)sizeof(float);   // K of the pixel pieces
     s.dp = o; o += ((D + 1 + 3) & ~3) * (int)sizeof(float);
+    s.ws = o; if (weighted) o += rsmax * (int)sizeof(float);
     s.bar = o; o += 2 * (int)sizeof(uint64_t);
     s.total = (o + 127) & ~127;
     return s;
@@ -203,7 +212,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     const int nline = xb ? g.height : g.width;
     const int npix = xb ? g.width : g.height;
     const int rs = rs_entries(npix);
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, WEIGHTED != 0);
     DdLine *rec = reinterpret_cast<DdLine *>(smem + L.rec);
     DdLine *drec = reinterpret_cast<DdLine *>(smem + L.drec);
     float2 *tab = reinterpret_cast<float2 *>(smem + L.tab);
@@ -211,7 +220,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     float *dps = reinterpret_cast<float *>(smem + L.dp);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     __shared__ int abort_flag;
-    __shared__ float wsum[NW];
+    __shared__ float wsum[BI * NW];
 
     const float2 *tsrc = xb ? it.tabx : it.taby;
     const size_t img_stride = (size_t)nline * rs;          // float2 per image
@@ -258,62 +267,62 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         if (WEIGHTED && np > 0) {
             // BackProjTransWeighted: multiply every pixel by its FBP weight at
             // this view (FanFlatDisCPU2d.cpp:693, FanArcDisCPU2d.cpp:703) and
-            // rebuild the line's prefix table in place (block scan).
+            // rebuild the line's prefix tables in place, all images in one
+            // block scan (the weights depend on the view, not on the image).
             float2 *tw = tab + (size_t)buf * BI * rsmax;
+            float *ws = reinterpret_cast<float *>(smem + L.ws);   // this thread's pixels only
             const float lpos = xb
-                ? (float)(((double)g.height / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift)
-                : (float)(((double)line - g.width / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
-            for (int b = 0; b < nb; b++) {
-                float2 *t = tw + (size_t)b * rsmax;
-                constexpr int kPer = 16;   // npix <= 4096
-                const int per = (npix + (NW * 32) - 1) / (NW * 32);
-                float yv[kPer];
-                float run = 0.0f;
-#pragma unroll
-                for (int q = 0; q < kPer; q++) {
-                    const int i = tid * per + q;
-                    float y = 0.0f;
-                    if (q < per && i < npix) {
-                        float pcx, pcy;
-                        if (xb) {
-                            pcx = (float)(((double)i + 0.5) * (double)g.pix_x + (double)vw.axis0);
-                            pcy = lpos;
-                        } else {
-                            pcx = lpos;
-                            pcy = (float)(((double)i + 0.5) * (double)g.pix_y + (double)vw.axis0);
-                        }
-                        const float w = (GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
-                                                              : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
-                        y = t[i].y * w;
-                    }
-                    yv[q] = y;
-                    run += y;
+                ? pix_centre(0.5f * (float)g.height - (float)line - 0.5f, g.pix_y, g.pix_yshift)
+                : pix_centre((float)line - 0.5f * (float)g.width + 0.5f, g.pix_x, g.pix_xshift);
+            const int per = (npix + (NW * 32) - 1) / (NW * 32);   // consecutive pixels per thread
+            const int i0 = tid * per, i1 = min(i0 + per, npix);
+            for (int i = i0; i < i1; i++) {
+                float pcx, pcy;
+                if (xb) {
+                    pcx = pix_centre((float)i + 0.5f, g.pix_x, vw.axis0);
+                    pcy = lpos;
+                } else {
+                    pcx = lpos;
+                    pcy = pix_centre((float)i + 0.5f, g.pix_y, vw.axis0);
                 }
-                float inc = run;
+                ws[i] = (GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
+                                              : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+            }
+            float run[BI], inc[BI];
+#pragma unroll
+            for (int b = 0; b < BI; b++) {
+                run[b] = 0.0f;
+                if (b < nb) {
+                    const float2 *t = tw + (size_t)b * rsmax;
+                    for (int i = i0; i < i1; i++) run[b] += t[i].y * ws[i];
+                }
+                inc[b] = run[b];
                 for (int o = 1; o < 32; o <<= 1) {
-                    const float z = __shfl_up_sync(0xffffffffu, inc, o);
-                    if (lane >= o) inc += z;
+                    const float z = __shfl_up_sync(0xffffffffu, inc[b], o);
+                    if (lane >= o) inc[b] += z;
                 }
-                if (lane == 31) wsum[warp] = inc;
-                __syncthreads();
-                float wbase = 0.0f;
-                for (int w = 0; w < warp; w++) wbase += wsum[w];
-                float pre = wbase + inc - run;
+                if (lane == 31) wsum[b * NW + warp] = inc[b];
+            }
+            __syncthreads();
 #pragma unroll
-                for (int q = 0; q < kPer; q++) {
-                    const int i = tid * per + q;
-                    if (q < per && i < npix) {
-                        t[i] = make_float2(pre, yv[q]);
-                        pre += yv[q];
-                    }
+            for (int b = 0; b < BI; b++) {
+                if (b >= nb) break;
+                float2 *t = tw + (size_t)b * rsmax;
+                float wbase = 0.0f;
+                for (int w = 0; w < warp; w++) wbase += wsum[b * NW + w];
+                float pre = wbase + inc[b] - run[b];
+                for (int i = i0; i < i1; i++) {
+                    const float y = t[i].y * ws[i];
+                    t[i] = make_float2(pre, y);
+                    pre += y;
                 }
                 if (tid == (NW * 32) - 1) {
                     float tot = 0.0f;
-                    for (int w = 0; w < NW; w++) tot += wsum[w];
+                    for (int w = 0; w < NW; w++) tot += wsum[b * NW + w];
                     t[npix] = make_float2(tot, 0.0f);
                 }
-                __syncthreads();
             }
+            __syncthreads();
         }
         if (np > 0) {
             const float2 *tb = tab + (size_t)buf * BI * rsmax;
@@ -642,11 +651,11 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
             if (OPK == 2 && valid) {
                 float pcx, pcy;
                 if (vw.xb) {
-                    pcx = (float)(((double)pi + 0.5) * (double)g.pix_x + (double)vw.axis0);
-                    pcy = (float)(((double)H / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift);
+                    pcx = pix_centre((float)pi + 0.5f, g.pix_x, vw.axis0);
+                    pcy = pix_centre(0.5f * (float)H - (float)line - 0.5f, g.pix_y, g.pix_yshift);
                 } else {
-                    pcx = (float)(((double)line - W / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
-                    pcy = (float)(((double)pi + 0.5) * (double)g.pix_y + (double)vw.axis0);
+                    pcx = pix_centre((float)line - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
+                    pcy = pix_centre((float)pi + 0.5f, g.pix_y, vw.axis0);
                 }
                 wgt = alpha * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
                                                      : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
@@ -875,6 +884,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         const int2 *mp = reinterpret_cast<const int2 *>(mapb + (size_t)buf * kMapBlkBytes);
         const float *alb = reinterpret_cast<const float *>(mp + kTile * kMapE);   // line scales
         const float2 *sb = stage + (size_t)buf * kBI * kStage;
+        DdView2 vw;   // BackProjWeighted: the view's source and first pixel edge
+        if (OPK == 2) vw = it.views[v];
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) {
             const int r = r0 + warp + kWarps * q, c = c0 + lane;
@@ -891,15 +902,14 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             if (up.x < 0 || low.x < 0) continue;
             float wgt = (OPK == 0) ? 1.0f : alb[lr];
             if (OPK == 2) {
-                const DdView2 vw = it.views[v];
                 const int line = xb ? r : c, pi = xb ? c : H - 1 - r;
                 float pcx, pcy;
                 if (xb) {
-                    pcx = (float)(((double)pi + 0.5) * (double)g.pix_x + (double)vw.axis0);
-                    pcy = (float)(((double)H / 2.0 - line - 0.5) * (double)g.pix_y + (double)g.pix_yshift);
+                    pcx = pix_centre((float)pi + 0.5f, g.pix_x, vw.axis0);
+                    pcy = pix_centre(0.5f * (float)H - (float)line - 0.5f, g.pix_y, g.pix_yshift);
                 } else {
-                    pcx = (float)(((double)line - W / 2.0 + 0.5) * (double)g.pix_x + (double)g.pix_xshift);
-                    pcy = (float)(((double)pi + 0.5) * (double)g.pix_y + (double)vw.axis0);
+                    pcx = pix_centre((float)line - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
+                    pcy = pix_centre((float)pi + 0.5f, g.pix_y, vw.axis0);
                 }
                 wgt = wgt * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
                                                    : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
