@@ -219,14 +219,18 @@ DD_HD float dd3_line_mag(const DdView3 *w, float lpos) {
     return w->xb ? FDIV(w->srcy, FSUB(w->srcy, lpos)) : FDIV(w->srcx, FSUB(w->srcx, lpos));
 }
 
-// Pixel centre of pixel j on a line (the FBP weight is evaluated there).
+// Pixel centre of pixel j on a line (the FBP weight is evaluated there).  The
+// reference evaluates (j + 0.5) * pitch + axis0 in FP64 and rounds to FP32;
+// one FMA of the exact j + 0.5 rounds the exact value once, the same float
+// unless it lies within 2^-53 (relative) of an FP32 rounding boundary, at the
+// FP32 rate (this runs once per segment and view).
 DD_HD void dd3_pix_centre(const dd_geom3d *g, const DdView3 *w, float lpos, int j, float *px, float *py) {
     if (w->xb) {
-        *px = (float)DADD(DMUL(DADD((double)j, 0.5), (double)g->pix_x), (double)w->axis0);
+        *px = fmaf((float)j + 0.5f, g->pix_x, w->axis0);
         *py = lpos;
     } else {
         *px = lpos;
-        *py = (float)DADD(DMUL(DADD((double)j, 0.5), (double)g->pix_y), (double)w->axis0);
+        *py = fmaf((float)j + 0.5f, g->pix_y, w->axis0);
     }
 }
 
