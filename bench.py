@@ -278,7 +278,7 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
         flops = 2.0 * B * V * 736 * 736
         out["fbp_16x512_720v"] = {
             "what": "projector2d.filtered_backprojection of the 16 headline sinograms (cosine weight + ramp "
-                    "filter fused in one kernel, then the weighted DD back-projection, exact-adjoint family)",
+                    "filter fused in one kernel, then the weighted DD back-projection)",
             "ms_per_call": ms, "value": B / (ms / 1e3), "unit": "FBP/s",
             "ms_per_call_torch_conv2d_composition": ms_conv,
             "filter_kernel_ms": fms, "filter_kernel_TFLOPs_fp32": flops / (fms / 1e3) / 1e12}

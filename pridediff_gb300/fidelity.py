@@ -1,0 +1,112 @@
+"""PrideDiff's data-consistency block on this library (model/pridediff.py:9-68).
+
+PrideDiff builds one fan-arc projector (512^2 pixels of 0.7433 mm, 768
+detectors of 1.2858 mm, iso_source 595, source_detector 490.6, 720 views
+over 2 pi), takes A = projection and AT = filtered_backprojection, wraps them
+in autograd Functions whose backward is the other operator (``prj_fun``:
+forward A, backward FBP; ``prj_t_fun``: forward FBP, backward A) and computes
+
+    out = x - w * AT(A x - y)
+
+with one learned scalar w (``fidelity_module``).  ``FidelityModule`` keeps
+that behaviour (``adjoint="fbp"``) or uses the exact matched adjoint instead
+(``adjoint="exact"``: AT = ProjTrans, so that w * AT(A x - y) is a gradient
+step on ||A x - y||^2 / 2 and the backward of A is its true transpose).
+``fidelity_graph`` captures steps of the block in one CUDA graph, as a
+sampling loop would replay it between network evaluations.
+"""
+from __future__ import annotations
+
+import torch
+import torch.nn as nn
+from torch.autograd import Function
+
+from .projector import projector2d
+
+
+def pridediff_projector() -> projector2d:
+    """The projector model/pridediff.py:9-14 builds."""
+    return projector2d(image_size=512, num_det=768, pix_size=0.7433, det_size=1.2858, iso_source=595.0,
+                       source_detector=490.6, scan_type="arc")
+
+
+def pridediff_views(device=None) -> torch.Tensor:
+    """model/pridediff.py:16: 720 views over 2 pi."""
+    return torch.arange(720, device=device) * torch.pi * 2 / 720
+
+
+class _Prj(Function):
+    """prj_fun: forward A, backward the module's adjoint (FBP in PrideDiff)."""
+
+    @staticmethod
+    def forward(ctx, image, mod):
+        ctx.mod = mod
+        return mod.proj.projection(image, mod.views)
+
+    @staticmethod
+    def backward(ctx, grad):
+        return ctx.mod.adjoint_op(grad.contiguous()), None
+
+
+class _PrjT(Function):
+    """prj_t_fun: forward the module's adjoint, backward A."""
+
+    @staticmethod
+    def forward(ctx, sino, mod):
+        ctx.mod = mod
+        return mod.adjoint_op(sino)
+
+    @staticmethod
+    def backward(ctx, grad):
+        return ctx.mod.proj.projection(grad.contiguous(), ctx.mod.views), None
+
+
+class FidelityModule(nn.Module):
+    """out = x - weight * AT(A x - proj).
+
+    proj / views default to PrideDiff's projector and views; adjoint is
+    "fbp" (PrideDiff: filtered_backprojection) or "exact" (ProjTrans).
+    PrideDiff allocates the weight uninitialised and loads it from a
+    checkpoint; here it starts at 0 until set or loaded (its state_dict key
+    is ``weight``, as in PrideDiff; the projector's tensors sit under
+    ``proj.``).
+    """
+
+    def __init__(self, proj: projector2d = None, views: torch.Tensor = None, adjoint: str = "fbp"):
+        super().__init__()
+        if adjoint not in ("fbp", "exact"):
+            raise ValueError(f"adjoint must be 'fbp' or 'exact', not {adjoint!r}")
+        self.weight = nn.Parameter(torch.zeros(()))
+        self.proj = proj if proj is not None else pridediff_projector()
+        self.register_buffer("views", views if views is not None else pridediff_views(), persistent=False)
+        self.adjoint = adjoint
+
+    def adjoint_op(self, sino: torch.Tensor) -> torch.Tensor:
+        if self.adjoint == "fbp":
+            return self.proj.filtered_backprojection(sino, self.views)
+        return self.proj.projection_t(sino, self.views)
+
+    def forward(self, input_data: torch.Tensor, proj: torch.Tensor, t=None) -> torch.Tensor:
+        temp = _Prj.apply(input_data, self) - proj
+        intervening_res = _PrjT.apply(temp, self)
+        return input_data - self.weight * intervening_res
+
+
+def fidelity_graph(module: FidelityModule, x: torch.Tensor, y: torch.Tensor, steps: int = 1):
+    """Capture `steps` applications x <- module(x, y) (in place, no autograd)
+    in one CUDA graph; replay it to run them."""
+    with torch.no_grad():
+        module(x.clone(), y)   # warm-up: plans, tables and kernel attributes
+    torch.cuda.synchronize(x.device)
+    graph = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream(x.device)
+    s.wait_stream(torch.cuda.current_stream(x.device))
+    with torch.no_grad(), torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            for _ in range(steps):
+                x.copy_(module(x, y))
+    torch.cuda.current_stream(x.device).wait_stream(s)
+    return graph
+
+
+__all__ = ["FidelityModule", "fidelity_graph", "pridediff_projector", "pridediff_views"]
