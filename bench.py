@@ -14,7 +14,9 @@ Metric: FP+BP per second (slice forward + adjoint pairs per second).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
 
 On one GPU the line also carries `extra`: the same slices through the plain
-per-slice path (the unbatched comparator), the 24-instance uneven batched
+per-slice path (the unbatched comparator), the FBP of the 16 sinograms (fused
+weight + filter kernel, then the weighted back-projection, beside the
+reference's torch-convolution composition), the 24-instance uneven batched
 data-consistency loop captured in a CUDA graph, and the 3-D cone-flat and
 spiral configurations, each with its view-swept bytes against the measured
 HBM peak.
