@@ -137,7 +137,7 @@ typedef struct dd_instance2d {
 
 /* tuning of the persistent launches (chosen by the autotuner) */
 typedef struct dd_tune2d {
-    int ctas_per_sm;  /* persistent CTAs per SM (1..4; 0 = default 2) */
+    int ctas_per_sm;  /* persistent CTAs per SM (0 = as many as fit; capped at that) */
     int lpt_order;    /* items longest-first (1) or in instance order (0) */
     int reserved[6];
 } dd_tune2d;

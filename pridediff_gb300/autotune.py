@@ -105,7 +105,8 @@ def recorded(key: str, path: Optional[str] = None) -> Dict[str, float]:
 # ---------------------------------------------------------------------------
 # GPU problems
 # ---------------------------------------------------------------------------
-BATCH_CANDIDATES = [{"ctas_per_sm": c, "lpt_order": o} for c in (1, 2, 3) for o in (1, 0)]
+# ctas_per_sm 0: as many persistent CTAs as fit on an SM
+BATCH_CANDIDATES = [{"ctas_per_sm": c, "lpt_order": o} for c in (0, 2, 4) for o in (1, 0)]
 
 
 def gpu_signature(device) -> dict:

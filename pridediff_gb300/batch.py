@@ -63,7 +63,7 @@ class UnevenBatch2d:
 
     # -- configuration -------------------------------------------------------
     def set_tune(self, tune: dict):
-        self.tune.ctas_per_sm = int(tune.get("ctas_per_sm", 2))
+        self.tune.ctas_per_sm = int(tune.get("ctas_per_sm", 0))
         self.tune.lpt_order = int(tune.get("lpt_order", 1))
         self.tune_dict = {"ctas_per_sm": self.tune.ctas_per_sm, "lpt_order": self.tune.lpt_order}
         if hasattr(self, "plan"):

@@ -307,9 +307,25 @@ static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
     return DD_OK;
 }
 
+// Persistent grid: CTAs per SM as the tuning asks, at most as many as fit
+// (`fit`, from the kernel's registers and shared memory); 0 = as many as fit.
+static int grid_of(const dd_tune2d *t, int nitems, int fit) {
+    int per = (t && t->ctas_per_sm > 0) ? t->ctas_per_sm : fit;
+    if (per > fit) per = fit;
+    if (per < 1) per = 1;
+    return std::max(1, std::min(nitems, per * sm_count()));
+}
+
+template <typename K>
+static int resident_ctas(K kern, int smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kThreads, (size_t)smem) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
 template <int GEOM>
 static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
-                            float *out, const float *sub, int *counter, int *status, int grid,
+                            float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
     const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax);
     auto kern = k_fwd_items<GEOM, 8>;
@@ -322,6 +338,7 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
+    const int grid = grid_of(tune, L.nfwd, resident_ctas(kern, S.total));
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
     kern<<<grid, kThreads, S.total, st>>>(op, (const BatchInst *)(planb + L.desc),
                                           (const int4 *)(planb + L.fitems), L.nfwd, planb, L.plans, tabs,
@@ -334,11 +351,12 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
 template <int GEOM>
 static int launch_adj_items(int op, const BatchLayout &L, const char *planb, const float2 *dtabs,
                             float *out, const float *base, float scale, int *counter, int *status,
-                            int grid, cudaStream_t st) {
+                            const dd_tune2d *tune, cudaStream_t st) {
     const AdjSmem S = adj_smem(GEOM);
     auto kern = (op == DD_OP_PROJ_T) ? k_adj_items<GEOM, 0> : k_adj_items<GEOM, 1>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
+    const int grid = grid_of(tune, L.nadj, resident_ctas(kern, S.total));
     ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
     kern<<<grid, kThreads, S.total, st>>>((const BatchInst *)(planb + L.desc),
                                           (const int4 *)(planb + L.aitems), L.nadj, planb, L.plans, dtabs,
@@ -346,12 +364,6 @@ static int launch_adj_items(int op, const BatchLayout &L, const char *planb, con
     prof_end(pr, st);
     count_launches(1);
     return launch_status();
-}
-
-static int grid_of(const dd_tune2d *t, int nitems) {
-    int per = (t && t->ctas_per_sm > 0) ? t->ctas_per_sm : 2;
-    if (per > 4) per = 4;
-    return std::max(1, std::min(nitems, per * sm_count()));
 }
 
 // forward of all instances: out = A in (- sub)
@@ -374,10 +386,9 @@ static int batch_forward(int scan, int op, const BatchLayout &L, const char *pla
     prof_end(pr, st);
     count_launches(2);
     if (cudaMemsetAsync(counter, 0, 2 * sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
-    const int grid = grid_of(tune, L.nfwd);
-    if (geom == DD_GEOM_PARA) return launch_fwd_items<DD_GEOM_PARA>(op, L, planb, tabs, out, sub, counter, status, grid, st);
-    if (geom == DD_GEOM_FLAT) return launch_fwd_items<DD_GEOM_FLAT>(op, L, planb, tabs, out, sub, counter, status, grid, st);
-    return launch_fwd_items<DD_GEOM_ARC>(op, L, planb, tabs, out, sub, counter, status, grid, st);
+    if (geom == DD_GEOM_PARA) return launch_fwd_items<DD_GEOM_PARA>(op, L, planb, tabs, out, sub, counter, status, tune, st);
+    if (geom == DD_GEOM_FLAT) return launch_fwd_items<DD_GEOM_FLAT>(op, L, planb, tabs, out, sub, counter, status, tune, st);
+    return launch_fwd_items<DD_GEOM_ARC>(op, L, planb, tabs, out, sub, counter, status, tune, st);
 }
 
 // adjoint of all instances: out = base + scale * (A^T in)   (base may be null)
@@ -398,10 +409,9 @@ static int batch_adjoint(int scan, int op, const BatchLayout &L, const char *pla
     prof_end(pr, st);
     count_launches(1);
     if (cudaMemsetAsync(counter, 0, 2 * sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
-    const int grid = grid_of(tune, L.nadj);
-    if (geom == DD_GEOM_PARA) return launch_adj_items<DD_GEOM_PARA>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
-    if (geom == DD_GEOM_FLAT) return launch_adj_items<DD_GEOM_FLAT>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
-    return launch_adj_items<DD_GEOM_ARC>(op, L, planb, dtabs, out, base, scale, counter, status, grid, st);
+    if (geom == DD_GEOM_PARA) return launch_adj_items<DD_GEOM_PARA>(op, L, planb, dtabs, out, base, scale, counter, status, tune, st);
+    if (geom == DD_GEOM_FLAT) return launch_adj_items<DD_GEOM_FLAT>(op, L, planb, dtabs, out, base, scale, counter, status, tune, st);
+    return launch_adj_items<DD_GEOM_ARC>(op, L, planb, dtabs, out, base, scale, counter, status, tune, st);
 }
 
 }  // namespace dd2
