@@ -504,6 +504,7 @@ def main():
     dom_ms = kern.get(dom, {}).get("ms_per_launch", float("nan"))
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     traffic = ncu_traffic().get(dom)
+    compulsory = 4.0 * B * (512 * 512 + V * 736)         # image in + sinogram out (or back)
 
     # ---- end to end through the public API with host buffers
     x_host = x0.detach().cpu().pin_memory()
@@ -546,7 +547,12 @@ def main():
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "fallback 6.8 TB/s",
                          "algorithmic_bytes_per_launch": alg_bytes,
-                         "bytes_model": "view-swept 4*V*(H*W + D) per slice per operator"},
+                         "bytes_model": "view-swept 4*V*(H*W + D) per slice per operator",
+                         # the compulsory bytes of one launch (inputs + outputs once) and the
+                         # (view, pixel) incidences per second of the whole step
+                         "compulsory_bytes_per_launch": compulsory,
+                         "compulsory_frac": compulsory / (dom_ms / 1e3) / 1e9 / peak,
+                         "incidences_per_s": 2.0 * world * B * V * 512 * 512 / (ms / 1e3)},
             "kernels": kern,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(x_host.numel() * 4 + y_host.numel() * 4),
