@@ -72,29 +72,18 @@ __global__ void k_lines(int geom, dd_geom2d g, const float *__restrict__ angles,
 // ---------------------------------------------------------------------------
 // Prefix tables
 // ---------------------------------------------------------------------------
-// Row lines (x-branch): one warp per (image, row); S_j = sum_{i<j} x_i in FP64,
-// rounded once.  Entry n = (S_n, 0).
+// Row lines (x-branch): one warp per (image, row); S_j = sum_{i<j} x_i in
+// double-float arithmetic, rounded once.  Entry n = (S_n, 0).
 __global__ void k_tab_rows(const float *__restrict__ img, int B, int H, int W,
                            float2 *__restrict__ tab) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= B * H) return;
     const float *row = img + (size_t)warp * W;
-    float2 *t = tab + (size_t)warp * rs_entries(W);
-    double run = 0.0;
-    for (int j0 = 0; j0 <= W; j0 += 32) {
-        const int j = j0 + lane;
-        const float x = (j < W) ? row[j] : 0.0f;
-        double inc = (double)x;
-        // inclusive warp scan
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        const double excl = run + inc - (double)x;
-        if (j <= W) t[j] = make_float2((float)excl, x);
-        run += __shfl_sync(0xffffffffu, inc, 31);
-    }
+    warp_prefix_table(W, tab + (size_t)warp * rs_entries(W), lane, [&](int j, float *x, float *w) {
+        *x = row[j];
+        *w = 1.0f;
+    });
 }
 
 // Column lines (y-branch): line = image column, walked from the bottom row.
@@ -106,13 +95,13 @@ __global__ void k_tab_cols(const float *__restrict__ img, int B, int H, int W,
     const int b = idx / W, col = idx - b * W;
     const float *im = img + (size_t)b * H * W;
     float2 *t = tab + (size_t)idx * rs_entries(H);
-    double run = 0.0;
+    DdF run = {0.0f, 0.0f};
     for (int i = 0; i < H; i++) {
         const float x = im[(size_t)(H - 1 - i) * W + col];
-        t[i] = make_float2((float)run, x);
-        run += (double)x;
+        t[i] = make_float2(run.hi, x);
+        run = df_add(run, DdF{x, 0.0f});
     }
-    t[H] = make_float2((float)run, 0.0f);
+    t[H] = make_float2(run.hi, 0.0f);
 }
 
 // Detector tables for the adjoint: per (image, view) G_k and g_k over the
@@ -131,32 +120,17 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
     const float *s = sino + ((size_t)b * V + v) * D;
     const float *dpv = dp + (size_t)v * (D + 1);
     const float *bc = bcoef + (size_t)v * (D + 1);
-    float2 *t = tab + (size_t)warp * rs_entries(D);
     const float pc = vw.xb ? para_coef_x : para_coef_y;
-    double run = 0.0;
-    for (int k0 = 0; k0 <= D; k0 += 32) {
-        const int k = k0 + lane;
-        float gk = 0.0f;
-        double w = 0.0;
-        if (k < D) {
-            const float sv = s[vw.flip ? D - 1 - k : k];
-            if (geom == DD_GEOM_PARA) {
-                gk = (mode == 0) ? sv * pc : sv;
-                w = 1.0;
-            } else {
-                gk = (mode == 0) ? sv * bc[k] : sv;
-                w = (double)(dpv[k + 1] - dpv[k]);
-            }
+    warp_prefix_table(D, tab + (size_t)warp * rs_entries(D), lane, [&](int k, float *g, float *w) {
+        const float sv = s[vw.flip ? D - 1 - k : k];
+        if (geom == DD_GEOM_PARA) {
+            *g = (mode == 0) ? sv * pc : sv;
+            *w = 1.0f;
+        } else {
+            *g = (mode == 0) ? sv * bc[k] : sv;
+            *w = dpv[k + 1] - dpv[k];
         }
-        double inc = (double)gk * w;
-        const double mine = inc;
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        if (k <= D) t[k] = make_float2((float)(run + inc - mine), gk);
-        run += __shfl_sync(0xffffffffu, inc, 31);
-    }
+    });
 }
 
 // Single-geometry forward launch: grid (views, image groups).

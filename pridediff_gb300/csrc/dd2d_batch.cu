@@ -114,19 +114,10 @@ __global__ void k_tab_rows_b(const BatchInst *__restrict__ desc, const float *__
     const int lane = threadIdx.x & 31;
     if (warp >= d.batch * H) return;
     const float *row = img + d.img_off + (size_t)warp * W;
-    float2 *t = tabs + d.tabx_off + (size_t)warp * rs_entries(W);
-    double run = 0.0;
-    for (int j0 = 0; j0 <= W; j0 += 32) {
-        const int j = j0 + lane;
-        const float x = (j < W) ? row[j] : 0.0f;
-        double inc = (double)x;
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        if (j <= W) t[j] = make_float2((float)(run + inc - (double)x), x);
-        run += __shfl_sync(0xffffffffu, inc, 31);
-    }
+    warp_prefix_table(W, tabs + d.tabx_off + (size_t)warp * rs_entries(W), lane, [&](int j, float *x, float *w) {
+        *x = row[j];
+        *w = 1.0f;
+    });
 }
 
 __global__ void k_tab_cols_b(const BatchInst *__restrict__ desc, const float *__restrict__ img,
@@ -138,13 +129,13 @@ __global__ void k_tab_cols_b(const BatchInst *__restrict__ desc, const float *__
     const int b = idx / W, col = idx - b * W;
     const float *im = img + d.img_off + (size_t)b * H * W;
     float2 *t = tabs + d.taby_off + (size_t)idx * rs_entries(H);
-    double run = 0.0;
+    DdF run = {0.0f, 0.0f};
     for (int i = 0; i < H; i++) {
         const float x = im[(size_t)(H - 1 - i) * W + col];
-        t[i] = make_float2((float)run, x);
-        run += (double)x;
+        t[i] = make_float2(run.hi, x);
+        run = df_add(run, DdF{x, 0.0f});
     }
-    t[H] = make_float2((float)run, 0.0f);
+    t[H] = make_float2(run.hi, 0.0f);
 }
 
 __global__ void k_dettab_b(int geom, int mode, const BatchInst *__restrict__ desc,
@@ -163,30 +154,16 @@ __global__ void k_dettab_b(int geom, int mode, const BatchInst *__restrict__ des
     const float *s = sino + d.sino_off + ((size_t)b * V + v) * D;
     float2 *t = dtabs + d.dtab_off + (size_t)warp * rs_entries(D);
     const float pc = vw.xb ? d.g.pix_y / d.g.det_size : d.g.pix_x / d.g.det_size;
-    double run = 0.0;
-    for (int k0 = 0; k0 <= D; k0 += 32) {
-        const int k = k0 + lane;
-        float gk = 0.0f;
-        double w = 0.0;
-        if (k < D) {
-            const float sv = s[vw.flip ? D - 1 - k : k];
-            if (geom == DD_GEOM_PARA) {
-                gk = (mode == 0) ? sv * pc : sv;
-                w = 1.0;
-            } else {
-                gk = (mode == 0) ? sv * bc[k] : sv;
-                w = (double)(dpv[k + 1] - dpv[k]);
-            }
+    warp_prefix_table(D, t, lane, [&](int k, float *g, float *w) {
+        const float sv = s[vw.flip ? D - 1 - k : k];
+        if (geom == DD_GEOM_PARA) {
+            *g = (mode == 0) ? sv * pc : sv;
+            *w = 1.0f;
+        } else {
+            *g = (mode == 0) ? sv * bc[k] : sv;
+            *w = dpv[k + 1] - dpv[k];
         }
-        double inc = (double)gk * w;
-        const double mine = inc;
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        if (k <= D) t[k] = make_float2((float)(run + inc - mine), gk);
-        run += __shfl_sync(0xffffffffu, inc, 31);
-    }
+    });
 }
 
 // ---------------------------------------------------------------------------

@@ -136,6 +136,56 @@ __device__ __forceinline__ float piece_K(const DdLine &L, const float2 *tab, int
 // boundary -- and FP64 arithmetic runs at a small fraction of the FP32 rate.
 __device__ __forceinline__ float pix_centre(float a, float pitch, float shift) { return fmaf(a, pitch, shift); }
 
+// ---------------------------------------------------------------------------
+// Prefix tables in double-float arithmetic.  A sum is carried as an unevaluated
+// pair hi + lo of floats (two-sum and FMA two-product are exact), about 48
+// significant bits; hi of the pair is the sum rounded to FP32.  FP64 would do
+// the same, but GB300 runs FP64 at a small fraction of its FP32 rate and the
+// tables' scans were bound by it.
+// ---------------------------------------------------------------------------
+struct DdF {
+    float hi, lo;
+};
+__device__ __forceinline__ DdF df_add(DdF a, DdF b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float v = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    const float t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, t);
+    return {hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ DdF df_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DdF df_shfl_up(DdF a, int o) {
+    return {__shfl_up_sync(0xffffffffu, a.hi, o), __shfl_up_sync(0xffffffffu, a.lo, o)};
+}
+__device__ __forceinline__ DdF df_shfl(DdF a, int l) {
+    return {__shfl_sync(0xffffffffu, a.hi, l), __shfl_sync(0xffffffffu, a.lo, l)};
+}
+
+// One warp: entries k = 0 .. n of t get (sum_{m<k} v_m, x_k) for the values
+// v_k = x_k * w_k produced by val(k, &x, &w) (x = w = 0 past the end).
+template <typename F>
+__device__ __forceinline__ void warp_prefix_table(int n, float2 *t, int lane, F val) {
+    DdF run = {0.0f, 0.0f};
+    for (int k0 = 0; k0 <= n; k0 += 32) {
+        const int k = k0 + lane;
+        float x = 0.0f, w = 0.0f;
+        if (k < n) val(k, &x, &w);
+        DdF inc = df_prod(x, w);
+        for (int o = 1; o < 32; o <<= 1) {
+            const DdF y = df_shfl_up(inc, o);
+            if (lane >= o) inc = df_add(inc, y);
+        }
+        DdF prev = df_shfl_up(inc, 1);
+        if (lane == 0) prev = {0.0f, 0.0f};
+        if (k <= n) t[k] = make_float2(df_add(run, prev).hi, x);
+        run = df_add(run, df_shfl(inc, 31));
+    }
+}
+
 struct Loc {
     int p, j;
     float dl, r;
