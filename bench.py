@@ -506,26 +506,53 @@ def main():
     traffic = ncu_traffic().get(dom)
     compulsory = 4.0 * B * (512 * 512 + V * 736)         # image in + sinogram out (or back)
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public API with host buffers: every step copies
+    # its inputs in from pinned host memory and its gradient back out.  A copy
+    # stream moves step i + 1's inputs (into the other of two device buffers)
+    # and step i's gradient while the compute stream runs; the timed region runs
+    # from before the first input copy to after the last gradient copy and
+    # includes the L2 flush before every step.
     x_host = x0.detach().cpu().pin_memory()
     y_host = y.detach().cpu().pin_memory()
     g_host = torch.empty_like(x_host).pin_memory()
-    x_dev = torch.empty_like(x0)
-    y_dev = torch.empty_like(y)
-    e_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    xd = [torch.empty_like(x0) for _ in range(2)]
+    yd = [torch.empty_like(y) for _ in range(2)]
+    main = torch.cuda.current_stream(dev)
+    cs = torch.cuda.Stream(dev)
+    loaded = [torch.cuda.Event() for _ in range(2)]
+    freed = [torch.cuda.Event() for _ in range(2)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def load(i):
+        j = i % 2
+        with torch.cuda.stream(cs):
+            if i >= 2:
+                cs.wait_event(freed[j])   # step i - 2 is done with these buffers
+            xd[j].copy_(x_host, non_blocking=True)
+            yd[j].copy_(y_host, non_blocking=True)
+            loaded[j].record(cs)
+
     barrier()
     torch.cuda.synchronize()
+    t_start.record(main)
+    cs.wait_stream(main)
+    load(0)
     for i in range(args.steps):
+        j = i % 2
+        if i + 1 < args.steps:
+            load(i + 1)
         flush.fill_(float(i))
-        e_s[i].record()
-        x_dev.copy_(x_host, non_blocking=True)
-        y_dev.copy_(y_host, non_blocking=True)
-        g, _ = step(x_dev, y_dev)
-        g_host.copy_(g, non_blocking=True)
-        e_e[i].record()
+        main.wait_event(loaded[j])
+        g, _ = step(xd[j], yd[j])
+        freed[j].record(main)
+        with torch.cuda.stream(cs):
+            cs.wait_event(freed[j])
+            g.record_stream(cs)
+            g_host.copy_(g, non_blocking=True)
+    main.wait_stream(cs)
+    t_end.record(main)
     torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(e_s, e_e)) / args.steps, dev)
+    e2e_ms = max_over_ranks(t_start.elapsed_time(t_end) / args.steps, dev)
     e2e_value = world * B / (e2e_ms / 1e3)
 
     extras = None
