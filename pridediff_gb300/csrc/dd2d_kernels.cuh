@@ -302,7 +302,10 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         for (int b = 0; b < BI; b++) acc[m][b] = 0.0f;
 
     const float para_beta = xb ? FDIV(g.pix_y, g.det_size) : FDIV(g.pix_x, g.det_size);
-    if (tid == 0) issue(0, 0);
+    // the last warp issues the copies: the first warps build the piece
+    // constants right after the barrier, on every line's critical path
+    const int issuer = (NW - 1) * 32;
+    if (tid == issuer) issue(0, 0);
     for (int line = 0; line < nline; line++) {
         const int buf = line & 1;
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
@@ -311,7 +314,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         // takes the copies of line + 1
         __syncthreads();
         if (abort_flag) break;
-        if (tid == 0 && line + 1 < nline) issue(line + 1, buf ^ 1);
+        if (tid == issuer && line + 1 < nline) issue(line + 1, buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
         if (WEIGHTED && np > 0) {
