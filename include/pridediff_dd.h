@@ -128,7 +128,9 @@ int dd2d_dc_step(int scan, const dd_geom2d *g, const void *plan, float *x, const
  * is n instances of one scan type, each with its own geometry, view count and
  * number of slices.  Inputs and outputs are packed instance after instance:
  * images (batch_i, H_i, W_i), sinograms (batch_i, V_i, D_i).  Weighted
- * operators are not batched. */
+ * operators are not batched, and instances whose walked lines are too long
+ * for the persistent forward's shared memory (about 3,400 pixels) are refused
+ * with DD_ERR_SIZE_OVERFLOW (the single-geometry entry points take them). */
 typedef struct dd_instance2d {
     dd_geom2d geom;
     int num_view;

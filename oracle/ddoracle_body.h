@@ -227,6 +227,7 @@ static void FN(walk_view2)(const ddo_geom2 *g, int geom, int op, int v, T view,
             }
         }
         if (idet < 0) idet = 0; /* the reference reads out of bounds here */
+        if (ipix < 0) ipix = 0; /* likewise (a source inside the image); the kernels clamp too */
 
         T point1 = (T)(ipix + 1) * pint + p0;
         T det1 = 0;

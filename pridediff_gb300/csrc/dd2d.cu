@@ -142,7 +142,7 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
 constexpr int kFwdImages = 4;
 constexpr int kFwdWarps = 8;
 
-template <int GEOM, int WEIGHTED, int NPASS, int NW>
+template <int GEOM, int WEIGHTED, int NPASS, int NW, int BI>
 __global__ void __launch_bounds__(NW * 32)
 k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ views,
       const float *__restrict__ dp, const float *__restrict__ bcoef,
@@ -151,14 +151,14 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, kFwdImages, WEIGHTED != 0);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, WEIGHTED != 0);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     DdPhases ph;
     FwdItem it;
     it.v = blockIdx.x;
-    it.b0 = blockIdx.y * kFwdImages;
-    it.nb = min(kFwdImages, B - it.b0);
+    it.b0 = blockIdx.y * BI;
+    it.nb = min(BI, B - it.b0);
     it.V = V;
     it.nl = nl;
     it.views = views;
@@ -170,7 +170,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED, NPASS, kFwdImages, NW>(g, op, it, smem, g.num_det, rsmax, ph) && threadIdx.x == 0)
+    if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW>(g, op, it, smem, g.num_det, rsmax, ph) && threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
@@ -379,28 +379,51 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
     return launch_status();
 }
 
+// Largest dynamic shared memory a CTA may opt in to on this device.
+int max_smem_optin() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n <= 0)
+            n = 227 * 1024;   // no device to ask (host-side checks): the sm_103a figure
+    }
+    return n;
+}
+
+template <int GEOM, int BI>
+static auto fwd_kernel(bool w, int D) {
+    constexpr int NW = kFwdWarps;
+    auto kern = k_fwd<GEOM, 0, 8, NW, BI>;
+    switch (npass_class(D, NW)) {
+    case 1: kern = w ? k_fwd<GEOM, 1, 1, NW, BI> : k_fwd<GEOM, 0, 1, NW, BI>; break;
+    case 2: kern = w ? k_fwd<GEOM, 1, 2, NW, BI> : k_fwd<GEOM, 0, 2, NW, BI>; break;
+    case 3: kern = w ? k_fwd<GEOM, 1, 3, NW, BI> : k_fwd<GEOM, 0, 3, NW, BI>; break;
+    case 4: kern = w ? k_fwd<GEOM, 1, 4, NW, BI> : k_fwd<GEOM, 0, 4, NW, BI>; break;
+    default: kern = w ? k_fwd<GEOM, 1, 8, NW, BI> : k_fwd<GEOM, 0, 8, NW, BI>; break;
+    }
+    return kern;
+}
+
 template <int GEOM>
 static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const char *planb, int B,
                       int V, const float2 *tx, const float2 *ty, float *out, const float *sub,
                       int *status, cudaStream_t st) {
     const int rsmax = rs_entries(g->width > g->height ? g->width : g->height);
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, op == DD_OP_BPROJ_TW);
-    dim3 grid(V, (B + kFwdImages - 1) / kFwdImages);
+    const bool w = (op == DD_OP_BPROJ_TW);
+    // 4 images per CTA; 2 where the line tables of 4 would not fit in shared
+    // memory (lines of more than about 3,400 pixels)
+    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, w).total <= max_smem_optin() ? kFwdImages : 2;
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, w);
+    if (S.total > max_smem_optin()) return DD_ERR_SIZE_OVERFLOW;
+    dim3 grid(V, (B + bi - 1) / bi);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const float *bc = (const float *)(planb + P.bcoef);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    const bool w = (op == DD_OP_BPROJ_TW);
     constexpr int NW = kFwdWarps;
-    auto kern = k_fwd<GEOM, 0, 8, NW>;
-    switch (npass_class(g->num_det, NW)) {
-    case 1: kern = w ? k_fwd<GEOM, 1, 1, NW> : k_fwd<GEOM, 0, 1, NW>; break;
-    case 2: kern = w ? k_fwd<GEOM, 1, 2, NW> : k_fwd<GEOM, 0, 2, NW>; break;
-    case 3: kern = w ? k_fwd<GEOM, 1, 3, NW> : k_fwd<GEOM, 0, 3, NW>; break;
-    case 4: kern = w ? k_fwd<GEOM, 1, 4, NW> : k_fwd<GEOM, 0, 4, NW>; break;
-    default: kern = w ? k_fwd<GEOM, 1, 8, NW> : k_fwd<GEOM, 0, 8, NW>; break;
-    }
+    auto kern = (bi == kFwdImages) ? fwd_kernel<GEOM, kFwdImages>(w, g->num_det) : fwd_kernel<GEOM, 2>(w, g->num_det);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);

@@ -280,6 +280,10 @@ static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
         const int st = validate(scan, op, &inst[i].geom, inst[i].batch, inst[i].num_view);
         if (st != DD_OK) return st;
         if ((inst[i].geom.width + kTile - 1) / kTile > 0xFFFF) return DD_ERR_SIZE_OVERFLOW;
+        // the persistent forward stages 4 images' line tables per CTA
+        const dd_geom2d &g = inst[i].geom;
+        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height))).total > max_smem_optin())
+            return DD_ERR_SIZE_OVERFLOW;
     }
     return DD_OK;
 }

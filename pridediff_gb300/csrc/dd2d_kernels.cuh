@@ -1028,6 +1028,7 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
 int validate(int scan, int op, const dd_geom2d *g, int B, int V);
 int geom_of(int scan);
 int launch_status();
+int max_smem_optin();   // largest dynamic shared memory per CTA (opt-in) on this device
 // prefix tables of B images (forward) / B sinograms (adjoint) of one geometry
 int launch_image_tables(const dd_geom2d *g, const float *in, int B, float2 *tx, float2 *ty, cudaStream_t st);
 int launch_det_tables(int geom, int op, const dd_geom2d *g, const char *planb, const float *in, int B,
