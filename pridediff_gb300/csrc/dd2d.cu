@@ -25,6 +25,8 @@
 //   F(u) = K_p + dl_p * S_j + r * x_j
 // with a per-piece constant K_p computed once per line by a warp scan.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 #include <string.h>
 
@@ -172,6 +174,167 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.sub = sub;
     if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW>(g, op, it, smem, g.num_det, rsmax, ph) && threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
+}
+
+// Parallel beam (plan time): the views that walk image rows and those that
+// walk columns, each in view order.  One warp: ballots rank the views.
+__global__ void __launch_bounds__(32)
+k_axis_views(int V, const DdView2 *__restrict__ views, int *__restrict__ axisv) {
+    const int lane = threadIdx.x;
+    const unsigned below = (1u << lane) - 1u;
+    int nr = 0, nc = 0;
+    for (int v0 = 0; v0 < V; v0 += 32) {
+        const int v = v0 + lane;
+        const bool in = v < V;
+        const bool xb = in && views[v].xb;
+        const unsigned mr = __ballot_sync(0xffffffffu, xb), mc = __ballot_sync(0xffffffffu, in && !xb);
+        if (xb) axisv[2 + nr + __popc(mr & below)] = v;
+        else if (in) axisv[2 + V + nc + __popc(mc & below)] = v;
+        nr += __popc(mr);
+        nc += __popc(mc);
+    }
+    if (lane == 0) {
+        axisv[0] = nr;
+        axisv[1] = nc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Parallel-beam adjoint, line-major.  The parallel beam's detector boundaries
+// drift per walked line (ParaDisCPU2d.cpp:76, :100: the recurrence restarts
+// at each line's first bin), so every (view, line, image) needs its own piece
+// constants of the detector table.  One CTA takes one walked line and a group
+// of kBI images over all the views that walk its axis, builds the line's
+// piece constants once per view and serves all the line's pixels from them
+// (a 32 x 32 tile rebuilds them for each tile the line crosses).  A thread
+// owns fixed pixels of the line; their sums stay in shared memory.  The rows
+// (x-branch views) are written by one launch and the columns added by a
+// second, the same order as the tiled kernel's merge of its two ownerships,
+// with the same per-pixel arithmetic.
+// ---------------------------------------------------------------------------
+struct ParaSmem {
+    int rec, drec, tab, kt, acc, bar, total;
+};
+__host__ __device__ inline ParaSmem para_smem(int D, int npix) {
+    ParaSmem s;
+    int o = 0;
+    s.rec = o; o += 2 * (int)sizeof(DdLine);
+    s.drec = o; o += 2 * (int)sizeof(DdLine);
+    s.tab = o; o += 2 * kBI * rs_entries(D) * (int)sizeof(float2);
+    s.kt = o; o += kBI * 32 * (int)sizeof(float);
+    s.acc = o; o += ((kBI * npix + 3) & ~3) * (int)sizeof(float);
+    s.bar = o; o += 2 * (int)sizeof(uint64_t);
+    s.total = (o + 127) & ~127;
+    return s;
+}
+
+template <int OPK>   // 0 ProjTrans, 1 BackProj
+__global__ void __launch_bounds__(kThreads)
+k_adj_para(dd_geom2d g, int B, int V, int nl, int axis, const int *__restrict__ axisv,
+           const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines,
+           const float2 *__restrict__ dtab, float *__restrict__ out, const float *__restrict__ base,
+           float scale, int add, int *__restrict__ status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int W = g.width, H = g.height, D = g.num_det;
+    const int npix = axis ? W : H;
+    const int line = blockIdx.x, b0 = blockIdx.y * kBI, nb = min(kBI, B - b0);
+    const int nv = axisv[axis ? 0 : 1];
+    const int *vlist = axisv + 2 + (axis ? 0 : V);
+    const int rsd = rs_entries(D);
+    const ParaSmem S = para_smem(D, npix);
+    DdLine *rec = reinterpret_cast<DdLine *>(smem + S.rec);
+    DdLine *drec = reinterpret_cast<DdLine *>(smem + S.drec);
+    float2 *tabs = reinterpret_cast<float2 *>(smem + S.tab);   // [2][kBI][rsd]
+    float *kt = reinterpret_cast<float *>(smem + S.kt);        // [kBI][32]
+    float *accs = reinterpret_cast<float *>(smem + S.acc);     // [kBI][npix]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S.bar);
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < kBI * npix; i += kThreads) accs[i] = 0.0f;
+    if (tid == 0) abort_flag = 0;
+    init_bars(bar);   // synchronises the CTA
+    DdPhases ph;
+
+    const uint32_t rec_bytes = (uint32_t)sizeof(DdLine);
+    const uint32_t tab_bytes = (uint32_t)(rsd * sizeof(float2));
+    auto issue = [&](int idx, int buf) {
+        const int v = vlist[idx];
+        dd_mbar_expect_tx(&bar[buf], 2 * rec_bytes + nb * tab_bytes);
+        dd_bulk_g2s(rec + buf, lines + (size_t)v * nl + line, rec_bytes, &bar[buf]);
+        dd_bulk_g2s(drec + buf, dlines + (size_t)v * nl + line, rec_bytes, &bar[buf]);
+        for (int b = 0; b < nb; b++)
+            dd_bulk_g2s(tabs + ((size_t)buf * kBI + b) * rsd, dtab + ((size_t)(b0 + b) * V + v) * rsd, tab_bytes,
+                        &bar[buf]);
+    };
+    const int issuer = (kWarps - 1) * 32;
+    if (tid == issuer && nv > 0) issue(0, 0);
+    for (int idx = 0; idx < nv; idx++) {
+        const int buf = idx & 1;
+        if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
+        ph.flip(buf);
+        // past this barrier every warp has finished view idx - 1, whose
+        // buffer takes the copies of view idx + 1 (none is in flight on abort)
+        __syncthreads();
+        if (abort_flag) break;
+        if (tid == issuer && idx + 1 < nv) issue(idx + 1, buf ^ 1);
+        const DdLine &L = rec[buf], &Ld = drec[buf];
+        if (L.h.npiece == 0) continue;   // the same for the whole CTA
+        const int npd = Ld.h.npiece;
+        const float2 *tb = tabs + (size_t)buf * kBI * rsd;
+        for (int b = warp; b < nb; b += kWarps) kt[b * 32 + lane] = npd > 0 ? piece_K(Ld, tb + (size_t)b * rsd, lane) : 0.0f;
+        __syncthreads();
+        const int i0 = L.h.i0, nend = L.h.nend;
+        const float bound0 = L.h.bound0;
+        const float alpha = (OPK == 0) ? 1.0f : L.h.alpha;
+        for (int p0 = 0; p0 < npix; p0 += kThreads) {   // the same trip count for every thread
+            const int pi = p0 + tid;
+            const bool valid = pi < npix && pi >= i0 && pi < nend;
+            const bool need_low = valid && (lane == 0 || pi == i0);
+            float up = bound0, low = bound0;
+            if (valid) up = dd_boundary(&L, pi, L.p[0].Q + (float)(pi - L.p[0].gb) * L.p[0].dl);
+            if (need_low && pi > i0) low = dd_boundary(&L, pi - 1, L.p[0].Q + (float)(pi - 1 - L.p[0].gb) * L.p[0].dl);
+            int pU = 0, jU = 0, pL = 0, jL = 0;
+            float rU = 0.0f, rL = 0.0f, dlU = 0.0f, dlL = 0.0f;
+            if (npd > 0) {
+                const float uu = fminf(fmaxf(up, bound0), Ld.h.endv);
+                dd_locate(&Ld, uu, &pU, &jU, &rU);
+                dlU = Ld.p[pU].dl;
+                const float ul = fminf(fmaxf(low, bound0), Ld.h.endv);
+                dd_locate(&Ld, ul, &pL, &jL, &rL);
+                dlL = Ld.p[pL].dl;
+            }
+#pragma unroll
+            for (int b = 0; b < kBI; b++) {
+                if (b >= nb) break;
+                float hu = 0.0f, hl2 = 0.0f;
+                if (npd > 0) {
+                    const float2 e = tb[(size_t)b * rsd + jU];
+                    hu = fmaf(rU, e.y, fmaf(dlU, e.x, kt[b * 32 + pU]));
+                    if (need_low) {
+                        const float2 e2 = tb[(size_t)b * rsd + jL];
+                        hl2 = fmaf(rL, e2.y, fmaf(dlL, e2.x, kt[b * 32 + pL]));
+                    }
+                }
+                float hl = __shfl_up_sync(0xffffffffu, hu, 1);
+                if (need_low) hl = hl2;
+                if (valid) accs[b * npix + pi] += alpha * (hu - hl);
+            }
+        }
+    }
+    __syncthreads();
+    if (abort_flag) {
+        if (tid == 0) atomicExch(status, DD_ERR_TIMEOUT);
+        return;
+    }
+    for (int b = 0; b < nb; b++) {
+        for (int pi = tid; pi < npix; pi += kThreads) {
+            const int r = axis ? line : H - 1 - pi, c = axis ? pi : line;
+            const size_t o = ((size_t)(b0 + b) * H + r) * W + c;
+            const float val = accs[b * npix + pi];
+            if (!add) out[o] = base ? fmaf(scale, val, base[o]) : val;
+            else out[o] = base ? fmaf(scale, val, out[o]) : out[o] + val;
+        }
+    }
 }
 
 // Adjoint map of fan beams (plan time): one CTA per (tile, view) fills the
@@ -356,6 +519,10 @@ int plan(int scan, const dd_geom2d *g, const float *angles, int V, void *planp, 
     DdLine *dlines = scan == DD_SCAN_PARA ? (DdLine *)(base + P.dlines) : nullptr;
     ProfRec *pr = prof_begin(DD_KERNEL_PLAN, st);
     k_views<<<V, 256, 0, st>>>(geom, *g, angles, V, views, (float *)(base + P.ang), dp, bc);
+    if (geom == DD_GEOM_PARA) {
+        k_axis_views<<<1, 32, 0, st>>>(V, views, (int *)(base + P.axisv));
+        g_launches++;
+    }
     dim3 gl((P.nl + 63) / 64, V);
     k_lines<<<gl, 64, 0, st>>>(geom, *g, angles, V, P.nl, views, dp, lines, dlines);
     int n = 2;
@@ -457,6 +624,31 @@ static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     return launch_status();
 }
 
+// Parallel-beam adjoint: the rows' launch writes, the columns' launch adds.
+static int launch_adj_para(int op, const dd_geom2d *g, const PlanLayout &P, const char *planb, int B, int V,
+                           const float2 *dtab, float *out, const float *base, float scale, int *status,
+                           cudaStream_t st) {
+    const DdLine *lines = (const DdLine *)(planb + P.lines);
+    const DdLine *dlines = (const DdLine *)(planb + P.dlines);
+    const int *axisv = (const int *)(planb + P.axisv);
+    const int W = g->width, H = g->height, D = g->num_det;
+    const int smax = std::max(para_smem(D, W).total, para_smem(D, H).total);
+    if (smax > max_smem_optin()) return DD_ERR_SIZE_OVERFLOW;
+    auto kern = (op == DD_OP_PROJ_T) ? k_adj_para<0> : k_adj_para<1>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    ProfRec *pr = prof_begin(DD_KERNEL_ADJOINT, st);
+    for (int axis = 1; axis >= 0; axis--) {
+        const int npix = axis ? W : H, nline = axis ? H : W;
+        const dim3 grid((unsigned)nline, (unsigned)((B + kBI - 1) / kBI));
+        kern<<<grid, kThreads, para_smem(D, npix).total, st>>>(*g, B, V, P.nl, axis, axisv, lines, dlines, dtab,
+                                                                out, base, scale, axis == 0, status);
+    }
+    prof_end(pr, st);
+    g_launches += 2;
+    return launch_status();
+}
+
 int launch_image_tables(const dd_geom2d *g, const float *in, int B, float2 *tx, float2 *ty,
                         cudaStream_t st) {
     const int W = g->width, H = g->height;
@@ -511,7 +703,7 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
     const int ts = launch_det_tables(geom, op, g, planb, in, B, V, dtab, st);
     if (ts != DD_OK) return ts;
     if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
-    if (geom == DD_GEOM_PARA) return launch_adj<DD_GEOM_PARA>(op, g, P, planb, angles, B, V, dtab, out, base, scale, status, st);
+    if (geom == DD_GEOM_PARA) return launch_adj_para(op, g, P, planb, B, V, dtab, out, base, scale, status, st);
     if (geom == DD_GEOM_FLAT) return launch_adj<DD_GEOM_FLAT>(op, g, P, planb, angles, B, V, dtab, out, base, scale, status, st);
     return launch_adj<DD_GEOM_ARC>(op, g, P, planb, angles, B, V, dtab, out, base, scale, status, st);
 }

@@ -33,7 +33,7 @@ __host__ __device__ inline int rs_entries(int n) { return (n + 2) & ~1; }   // n
 // Workspace layout
 // ---------------------------------------------------------------------------
 struct PlanLayout {
-    size_t views, ang, dp, bcoef, lines, dlines, amap, trange, total;
+    size_t views, ang, dp, bcoef, lines, dlines, axisv, amap, trange, total;
     int nl;   // line records per view = max(H, W)
 };
 
@@ -72,6 +72,10 @@ inline PlanLayout plan_layout(int scan, const dd_geom2d *g, int V, bool with_map
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
     L.dlines = o;
     if (scan == DD_SCAN_PARA) o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl, 256);
+    // parallel beam: the views that walk rows and those that walk columns
+    // ({count rows, count columns, rows' views[V], columns' views[V]})
+    L.axisv = o;
+    if (scan == DD_SCAN_PARA) o = align_up(o + sizeof(int) * (2 * (size_t)V + 2), 256);
     L.amap = L.trange = o;
     if (scan != DD_SCAN_PARA && with_map) {
         L.amap = o; o = align_up(o + (size_t)kMapBlkBytes * V * tiles_n(g), 256);
