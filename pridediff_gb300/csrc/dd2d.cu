@@ -286,37 +286,30 @@ k_adj_para(dd_geom2d g, int B, int V, int nl, int axis, const int *__restrict__ 
         const int i0 = L.h.i0, nend = L.h.nend;
         const float bound0 = L.h.bound0;
         const float alpha = (OPK == 0) ? 1.0f : L.h.alpha;
-        for (int p0 = 0; p0 < npix; p0 += kThreads) {   // the same trip count for every thread
-            const int pi = p0 + tid;
-            const bool valid = pi < npix && pi >= i0 && pi < nend;
-            const bool need_low = valid && (lane == 0 || pi == i0);
-            float up = bound0, low = bound0;
-            if (valid) up = dd_boundary(&L, pi, L.p[0].Q + (float)(pi - L.p[0].gb) * L.p[0].dl);
-            if (need_low && pi > i0) low = dd_boundary(&L, pi - 1, L.p[0].Q + (float)(pi - 1 - L.p[0].gb) * L.p[0].dl);
-            int pU = 0, jU = 0, pL = 0, jL = 0;
-            float rU = 0.0f, rL = 0.0f, dlU = 0.0f, dlL = 0.0f;
+        // a warp takes 32 consecutive pixel boundaries (lane l: the upper
+        // boundary of pixel q0 + l - 1) and 31 pixels: each boundary is
+        // located once and neighbours difference by one shuffle
+        for (int q0 = warp * kBinsPerWarp; q0 < npix; q0 += kWarps * kBinsPerWarp) {   // warp-uniform
+            const int bi = q0 + lane - 1;   // boundary index (upper boundary of pixel bi)
+            float u = bound0;               // boundary i0 - 1 is the walk start; below it H is constant
+            if (bi >= i0 && bi < nend) u = dd_boundary(&L, bi, L.p[0].Q + (float)(bi - L.p[0].gb) * L.p[0].dl);
+            int pU = 0, jU = 0;
+            float rU = 0.0f, dlU = 0.0f;
             if (npd > 0) {
-                const float uu = fminf(fmaxf(up, bound0), Ld.h.endv);
-                dd_locate(&Ld, uu, &pU, &jU, &rU);
+                dd_locate(&Ld, fminf(fmaxf(u, bound0), Ld.h.endv), &pU, &jU, &rU);
                 dlU = Ld.p[pU].dl;
-                const float ul = fminf(fmaxf(low, bound0), Ld.h.endv);
-                dd_locate(&Ld, ul, &pL, &jL, &rL);
-                dlL = Ld.p[pL].dl;
             }
+            const int pi = bi;   // the pixel this lane closes (lanes 1..31)
+            const bool valid = lane > 0 && pi < npix && pi >= i0 && pi < nend;
 #pragma unroll
             for (int b = 0; b < kBI; b++) {
                 if (b >= nb) break;
-                float hu = 0.0f, hl2 = 0.0f;
+                float hu = 0.0f;
                 if (npd > 0) {
                     const float2 e = tb[(size_t)b * rsd + jU];
                     hu = fmaf(rU, e.y, fmaf(dlU, e.x, kt[b * 32 + pU]));
-                    if (need_low) {
-                        const float2 e2 = tb[(size_t)b * rsd + jL];
-                        hl2 = fmaf(rL, e2.y, fmaf(dlL, e2.x, kt[b * 32 + pL]));
-                    }
                 }
-                float hl = __shfl_up_sync(0xffffffffu, hu, 1);
-                if (need_low) hl = hl2;
+                const float hl = __shfl_up_sync(0xffffffffu, hu, 1);
                 if (valid) accs[b * npix + pi] += alpha * (hu - hl);
             }
         }
