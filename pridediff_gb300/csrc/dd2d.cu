@@ -31,6 +31,7 @@
 #include <string.h>
 
 #include "dd2d_kernels.cuh"
+#include "dd_trace.h"
 
 namespace dd2 {
 // ---------------------------------------------------------------------------
@@ -731,6 +732,7 @@ extern "C" size_t dd2d_workspace_bytes(int scan, int op, const dd_geom2d *g, int
 
 extern "C" int dd2d_plan(int scan, const dd_geom2d *g, const float *angles, int num_view, void *planp,
                          size_t plan_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_plan", scan, -1, false);
     const int st = validate(scan, DD_OP_PROJ, g, 1, num_view);
     if (st != DD_OK) return st;
     return plan(scan, g, angles, num_view, planp, plan_bytes, (cudaStream_t)stream);
@@ -739,6 +741,7 @@ extern "C" int dd2d_plan(int scan, const dd_geom2d *g, const float *angles, int 
 extern "C" int dd2d_apply(int scan, int op, const dd_geom2d *g, const float *in, float *out,
                           const float *angles, int batch, int num_view, void *workspace,
                           size_t workspace_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_apply", scan, op, false);
     const int st = validate(scan, op, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!angles || !in || !out) return DD_ERR_INVALID_ARG;
@@ -756,6 +759,7 @@ extern "C" int dd2d_apply(int scan, int op, const dd_geom2d *g, const float *in,
 extern "C" int dd2d_apply_planned(int scan, int op, const dd_geom2d *g, const void *planp,
                                   const float *in, float *out, int batch, int num_view,
                                   void *workspace, size_t workspace_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_apply_planned", scan, op, false);
     const int st = validate(scan, op, g, batch, num_view);
     if (st != DD_OK) return st;
     return apply_planned(scan, op, g, planp, in, out, batch, num_view, workspace, workspace_bytes,
@@ -773,6 +777,7 @@ extern "C" size_t dd2d_dc_workspace_bytes(int scan, const dd_geom2d *g, int batc
 extern "C" int dd2d_dc_step(int scan, const dd_geom2d *g, const void *planp, float *x, const float *y,
                             float *resid, float eta, int batch, int num_view, void *workspace,
                             size_t workspace_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_dc_step", scan, -1, false);
     const int st = validate(scan, DD_OP_PROJ, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!planp || !x || !y || !resid) return DD_ERR_INVALID_ARG;

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "dd2d_kernels.cuh"
+#include "dd_trace.h"
 
 namespace dd2 {
 
@@ -411,6 +412,7 @@ extern "C" size_t dd2d_batch_workspace_bytes(int scan, const dd_instance2d *inst
 
 extern "C" int dd2d_batch_plan(int scan, const dd_instance2d *inst, int n, const float *const *angles,
                                void *planp, size_t plan_bytes, const dd_tune2d *tune, dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_batch_plan", scan, -1, false);
     const int vs = validate_batch(scan, DD_OP_PROJ, inst, n);
     if (vs != DD_OK) return vs;
     if (!angles || !planp) return DD_ERR_INVALID_ARG;
@@ -466,6 +468,7 @@ extern "C" int dd2d_batch_plan(int scan, const dd_instance2d *inst, int n, const
 extern "C" int dd2d_batch_apply(int scan, int op, const dd_instance2d *inst, int n, const void *planp,
                                 const float *in, float *out, void *ws, size_t wsb, const dd_tune2d *tune,
                                 dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_batch_apply", scan, op, false);
     const int vs = validate_batch(scan, op, inst, n);
     if (vs != DD_OK) return vs;
     if (!planp || !in || !out) return DD_ERR_INVALID_ARG;
@@ -482,6 +485,7 @@ extern "C" int dd2d_batch_apply(int scan, int op, const dd_instance2d *inst, int
 extern "C" int dd2d_batch_dc_step(int scan, const dd_instance2d *inst, int n, const void *planp, float *x,
                                   const float *y, float eta, void *ws, size_t wsb, const dd_tune2d *tune,
                                   dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_batch_dc_step", scan, -1, false);
     const int vs = validate_batch(scan, DD_OP_PROJ, inst, n);
     if (vs != DD_OK) return vs;
     if (!planp || !x || !y) return DD_ERR_INVALID_ARG;

@@ -9,6 +9,7 @@
 // by an exclusive prefix sum -- to write them.  The entries come out in the
 // reference's order: view by view, line by line, step by step.
 #include "dd2d_kernels.cuh"
+#include "dd_trace.h"
 
 namespace dd2 {
 
@@ -57,6 +58,7 @@ extern "C" size_t dd2d_sysmatrix_lines(const dd_geom2d *g, int num_view) {
 
 extern "C" int dd2d_sysmatrix_count(int scan, const dd_geom2d *g, const void *plan, int num_view, long long *counts,
                                     dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_sysmatrix_count", scan, -1, false);
     if (!counts) return DD_ERR_INVALID_ARG;
     return sysmat_launch(scan, g, plan, num_view, counts, nullptr, nullptr, nullptr, nullptr, (cudaStream_t)stream);
 }
@@ -64,6 +66,7 @@ extern "C" int dd2d_sysmatrix_count(int scan, const dd_geom2d *g, const void *pl
 extern "C" int dd2d_sysmatrix_fill(int scan, const dd_geom2d *g, const void *plan, int num_view,
                                    const long long *offsets, long long *rows, long long *cols, float *vals,
                                    dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_sysmatrix_fill", scan, -1, false);
     if (!offsets || !rows || !cols || !vals) return DD_ERR_INVALID_ARG;
     return sysmat_launch(scan, g, plan, num_view, nullptr, offsets, rows, cols, vals, (cudaStream_t)stream);
 }

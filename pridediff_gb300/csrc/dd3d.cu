@@ -26,6 +26,7 @@
 #include "../../include/pridediff_dd.h"
 #include "dd_geom3d.cuh"
 #include "dd_tma.cuh"
+#include "dd_trace.h"
 
 namespace dd2 {   // launch accounting and profiling (dd2d.cu)
 struct ProfRec;
@@ -849,6 +850,7 @@ extern "C" size_t dd3d_plan_bytes(int scan, const dd_geom3d *g, int num_view) {
 
 extern "C" int dd3d_plan(int scan, const dd_geom3d *g, const float *angles, const float *source_pos, int num_view,
                          void *planp, size_t plan_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd3d_plan", scan, -1, true);
     const int st = validate(scan, DD_OP_PROJ, g, 1, num_view);
     if (st != DD_OK) return st;
     return plan(scan, g, angles, source_pos, num_view, planp, plan_bytes, (cudaStream_t)stream);
@@ -864,6 +866,7 @@ extern "C" size_t dd3d_apply_workspace_bytes(int scan, int op, const dd_geom3d *
 extern "C" int dd3d_apply_planned(int scan, int op, const dd_geom3d *g, const void *planp, const float *in,
                                   float *out, int batch, int num_view, void *workspace, size_t workspace_bytes,
                                   dd_stream_t stream) {
+    ddtrace::Range tr("dd3d_apply_planned", scan, op, true);
     const int st = validate(scan, op, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!planp || !in || !out) return DD_ERR_INVALID_ARG;
@@ -885,6 +888,7 @@ extern "C" size_t dd3d_workspace_bytes(int scan, int op, const dd_geom3d *g, int
 extern "C" int dd3d_apply(int scan, int op, const dd_geom3d *g, const float *in, float *out, const float *angles,
                           const float *source_pos, int batch, int num_view, void *workspace,
                           size_t workspace_bytes, dd_stream_t stream) {
+    ddtrace::Range tr("dd3d_apply", scan, op, true);
     const int st = validate(scan, op, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!in || !out || !angles || (scan == DD_SCAN_SPIRAL && !source_pos)) return DD_ERR_INVALID_ARG;
@@ -905,6 +909,7 @@ extern "C" size_t dd3d_dc_workspace_bytes(int scan, const dd_geom3d *g, int batc
 extern "C" int dd3d_dc_step(int scan, const dd_geom3d *g, const void *planp, float *x, const float *y, float *resid,
                             float eta, int batch, int num_view, void *workspace, size_t workspace_bytes,
                             dd_stream_t stream) {
+    ddtrace::Range tr("dd3d_dc_step", scan, -1, true);
     const int st = validate(scan, DD_OP_PROJ, g, batch, num_view);
     if (st != DD_OK) return st;
     if (!planp || !x || !y || !resid) return DD_ERR_INVALID_ARG;

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/pridediff_dd.h"
+#include "dd_trace.h"
 
 namespace dd2 {
 struct ProfRec;
@@ -102,6 +103,7 @@ using namespace ddfbp;
 
 extern "C" int dd_fbp_filter(const float *in, float *out, const float *weight, int wrows, const float *taps,
                              long long rows, int num_det, dd_stream_t stream) {
+    ddtrace::Range tr("dd_fbp_filter");
     if (!in || !out || !taps || rows <= 0 || num_det <= 0 || (weight && wrows <= 0)) return DD_ERR_INVALID_ARG;
     if (num_det > 8192 || (rows + kRows - 1) / kRows > 2147483647LL) return DD_ERR_SIZE_OVERFLOW;
     const size_t sb = smem_bytes(num_det);
