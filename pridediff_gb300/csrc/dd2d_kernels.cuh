@@ -306,6 +306,13 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         for (int b = 0; b < BI; b++) acc[m][b] = 0.0f;
 
     const float para_beta = xb ? FDIV(g.pix_y, g.det_size) : FDIV(g.pix_x, g.det_size);
+    // fan beams: each pass's detector boundary is the same for all the lines
+    // of the view; read it once
+    float ud[kMaxPass];
+#pragma unroll
+    for (int m = 0; m < kMaxPass; m++)
+        ud[m] = (GEOM != DD_GEOM_PARA && m < npass) ? dps[min(m * (NW * kBinsPerWarp) + warp * kBinsPerWarp + lane, D)]
+                                                     : 0.0f;
     // the last warp issues the copies: the first warps build the piece
     // constants right after the barrier, on every line's critical path
     const int issuer = (NW - 1) * 32;
@@ -401,7 +408,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                     const float est = Rd.p[0].Q + (float)(idx - Rd.p[0].gb) * Rd.p[0].dl;
                     u = (Rd.h.npiece > 0) ? dd_boundary(&Rd, idx, est) : bound0;
                 } else {
-                    u = dps[min(kb, D)];
+                    u = ud[m];
                 }
                 u = fminf(fmaxf(u, bound0), endv);
                 // 32 boundaries clamped to the same end of the walk give 31
