@@ -145,8 +145,9 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
 constexpr int kFwdImages = 4;
 constexpr int kFwdWarps = 8;
 
+// blockIdx.x = view * kFwdCluster + rank in the view's cluster.
 template <int GEOM, int WEIGHTED, int NPASS, int NW, int BI>
-__global__ void __launch_bounds__(NW * 32)
+__global__ void __cluster_dims__(kFwdCluster, 1, 1) __launch_bounds__(NW * 32)
 k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ views,
       const float *__restrict__ dp, const float *__restrict__ bcoef,
       const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines,
@@ -154,12 +155,12 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, WEIGHTED != 0);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, WEIGHTED != 0, kFwdCluster, NW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     DdPhases ph;
     FwdItem it;
-    it.v = blockIdx.x;
+    it.v = blockIdx.x / kFwdCluster;
     it.b0 = blockIdx.y * BI;
     it.nb = min(BI, B - it.b0);
     it.V = V;
@@ -173,7 +174,8 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW>(g, op, it, smem, g.num_det, rsmax, ph) && threadIdx.x == 0)
+    if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW, kFwdCluster>(g, op, it, smem, g.num_det, rsmax, ph) &&
+        threadIdx.x == 0)
         atomicExch(status, DD_ERR_TIMEOUT);
 }
 
@@ -574,16 +576,18 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     const bool w = (op == DD_OP_BPROJ_TW);
     // 4 images per CTA; 2 where the line tables of 4 would not fit in shared
     // memory (lines of more than about 3,400 pixels)
-    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, w).total <= max_smem_optin() ? kFwdImages : 2;
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, w);
+    constexpr int NW = kFwdWarps;
+    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, w, kFwdCluster, NW).total <= max_smem_optin()
+                       ? kFwdImages : 2;
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, w, kFwdCluster, NW);
     if (S.total > max_smem_optin()) return DD_ERR_SIZE_OVERFLOW;
-    dim3 grid(V, (B + bi - 1) / bi);
+    if ((long long)V * kFwdCluster > 0x7FFFFFFFLL) return DD_ERR_SIZE_OVERFLOW;
+    dim3 grid(V * kFwdCluster, (B + bi - 1) / bi);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const float *bc = (const float *)(planb + P.bcoef);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    constexpr int NW = kFwdWarps;
     auto kern = (bi == kFwdImages) ? fwd_kernel<GEOM, kFwdImages>(w, g->num_det) : fwd_kernel<GEOM, 2>(w, g->num_det);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;

@@ -178,38 +178,66 @@ __device__ __forceinline__ int next_item(int *counter) {
     return s_item;
 }
 
+// The forward's clusters: rank 0 takes the next item, the other ranks read its
+// index from rank 0's shared memory.  The second barrier keeps rank 0 (and
+// its s_item) in place until every rank has read it: past the last item rank
+// 0 exits, and a CTA's shared memory must not be read after it has exited.
+__device__ __forceinline__ int next_item_cluster(int *counter) {
+    __shared__ int s_item;
+    cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+    if (cluster.block_rank() == 0 && threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    cluster.sync();
+    const int i = *cluster.map_shared_rank(&s_item, 0);
+    cluster.sync();
+    return i;
+}
+
+// Resident CTAs per SM the persistent forward is compiled for: the plain
+// forward's register budget (40 per thread, 6 CTAs) up to 4 passes.
+__host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <= 4 ? 6 : 3; }
+
 template <int GEOM, int NPASS>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __cluster_dims__(kFwdCluster, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
 k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
             float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, false, kFwdCluster);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
+    // the item and its geometry live in shared memory: read where used, they
+    // hold no registers across the line loop (the plain forward reads them
+    // from kernel parameters)
+    __shared__ FwdItem s_it;
+    __shared__ dd_geom2d s_g;
     DdPhases ph;
     for (;;) {
-        const int i = next_item(counter);
+        const int i = next_item_cluster(counter);
         if (i >= nitems) break;
-        const int4 w = items[i];
-        const BatchInst &d = desc[w.x];
-        const char *pb = plan + plans_off + d.plan_off;
-        FwdItem it;
-        it.v = w.y;
-        it.b0 = w.z;
-        it.nb = w.w;
-        it.V = d.V;
-        it.nl = d.nl;
-        it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
-        it.dp = reinterpret_cast<const float *>(pb + d.dp);
-        it.bcoef = reinterpret_cast<const float *>(pb + d.bcoef);
-        it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
-        it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
-        it.tabx = tabs + d.tabx_off;
-        it.taby = tabs + d.taby_off;
-        it.out = out + d.sino_off;
-        it.sub = sub ? sub + d.sino_off : nullptr;
-        if (!fwd_view<GEOM, 0, NPASS>(d.g, op, it, smem, Dmax, rsmax, ph)) {
+        if (threadIdx.x == 0) {
+            const int4 w = items[i];
+            const BatchInst &d = desc[w.x];
+            const char *pb = plan + plans_off + d.plan_off;
+            FwdItem it;
+            it.v = w.y;
+            it.b0 = w.z;
+            it.nb = w.w;
+            it.V = d.V;
+            it.nl = d.nl;
+            it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
+            it.dp = reinterpret_cast<const float *>(pb + d.dp);
+            it.bcoef = reinterpret_cast<const float *>(pb + d.bcoef);
+            it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
+            it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
+            it.tabx = tabs + d.tabx_off;
+            it.taby = tabs + d.taby_off;
+            it.out = out + d.sino_off;
+            it.sub = sub ? sub + d.sino_off : nullptr;
+            s_it = it;
+            s_g = d.g;
+        }
+        __syncthreads();   // every thread passed the cluster barrier above before s_it changes
+        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }
@@ -283,7 +311,8 @@ static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
         if ((inst[i].geom.width + kTile - 1) / kTile > 0xFFFF) return DD_ERR_SIZE_OVERFLOW;
         // the persistent forward stages 4 images' line tables per CTA
         const dd_geom2d &g = inst[i].geom;
-        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height))).total > max_smem_optin())
+        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height)), kBI, false, kFwdCluster)
+                .total > max_smem_optin())
             return DD_ERR_SIZE_OVERFLOW;
     }
     return DD_OK;
@@ -305,11 +334,30 @@ static int resident_ctas(K kern, int smem) {
     return n;
 }
 
+// Persistent grid of a clustered kernel (clusters of `cl` CTAs): grid_of's CTA
+// count rounded down to whole clusters, at most the clusters that can be
+// resident at once.
+template <typename K>
+static int cluster_grid_of(const dd_tune2d *t, int nitems, K kern, int smem, int cl) {
+    const int ctas = grid_of(t, nitems * cl, resident_ctas(kern, smem));
+    int clusters = std::max(1, std::min(nitems, ctas / cl));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusters * cl);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    int maxc = 0;
+    if (cudaOccupancyMaxActiveClusters(&maxc, (void *)kern, &cfg) == cudaSuccess && maxc > 0)
+        clusters = std::min(clusters, maxc);
+    else
+        (void)cudaGetLastError();
+    return clusters * cl;
+}
+
 template <int GEOM>
 static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
                             float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
-    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax);
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, false, kFwdCluster);
     auto kern = k_fwd_items<GEOM, 8>;
     switch (npass_class(L.Dmax)) {
     case 1: kern = k_fwd_items<GEOM, 1>; break;
@@ -320,7 +368,7 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
-    const int grid = grid_of(tune, L.nfwd, resident_ctas(kern, S.total));
+    const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, kFwdCluster);
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
     kern<<<grid, kThreads, S.total, st>>>(op, (const BatchInst *)(planb + L.desc),
                                           (const int4 *)(planb + L.fitems), L.nfwd, planb, L.plans, tabs,

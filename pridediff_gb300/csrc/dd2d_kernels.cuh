@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cooperative_groups.h>
+
 #include "../../include/pridediff_dd.h"
 #include "dd_geom2d.cuh"
 #include "dd_tma.cuh"
@@ -210,18 +212,40 @@ __device__ __forceinline__ Loc locate(const DdLine &L, float u) {
 // lines with the line record and the kBI line tables double-buffered in
 // shared memory by TMA bulk copies.
 // ---------------------------------------------------------------------------
+// Detector passes of a 256-thread CTA (8 warps x 31 bins each) rounded up to
+// the instantiated classes; NPASS sizes the per-thread accumulators, so a
+// smaller class means fewer registers and more resident CTAs per SM.
+__host__ __device__ inline int npass_class(int D, int nw = kWarps) {
+    const int n = (D + nw * kBinsPerWarp - 1) / (nw * kBinsPerWarp);
+    return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : 8;
+}
+
 struct FwdSmem {
     // dynamic layout offsets (bytes)
     int rec, drec, tab, kt, dp, ws, bar, total;
 };
 
+// Forward CTAs per work item: a cluster of kFwdCluster CTAs shares a view's
+// lines (rank r walks lines r, r + kFwdCluster, ...), so items are shorter and
+// the last ones leave fewer SMs idle; rank 0 adds the others' sums through
+// distributed shared memory.
+constexpr int kFwdCluster = 2;
+
 // weighted: BackProjTransWeighted also keeps the FBP weights of a line's pixels.
-__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI, bool weighted = false) {
+// cl > 1: the line tables' space also holds a CTA's sums for the combine
+// (npass_class(D) passes x bi images x 32 lanes x nw warps floats).
+__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI, bool weighted = false,
+                                            int cl = 1, int nw = kWarps) {
     FwdSmem s;
     int o = 0;
     s.rec = o; o += 2 * (int)sizeof(DdLine);
     s.drec = o; if (geom == DD_GEOM_PARA) o += 2 * (int)sizeof(DdLine);
-    s.tab = o; o += 2 * bi * rsmax * (int)sizeof(float2);
+    s.tab = o;
+    {
+        const int tabs = 2 * bi * rsmax * (int)sizeof(float2);
+        const int red = cl > 1 ? npass_class(D, nw) * bi * nw * 32 * (int)sizeof(float) : 0;
+        o += tabs > red ? tabs : red;
+    }
     s.kt = o; o += bi * 32 * (int)sizeof(float);   // K of the pixel pieces
     s.dp = o; o += ((D + 1 + 3) & ~3) * (int)sizeof(float);
     s.ws = o; if (weighted) o += rsmax * (int)sizeof(float);
@@ -243,30 +267,26 @@ struct FwdItem {
     const float *sub;            // optional, same layout as out
 };
 
-// Detector passes of a 256-thread CTA (8 warps x 31 bins each) rounded up to
-// the instantiated classes; NPASS sizes the per-thread accumulators, so a
-// smaller class means fewer registers and more resident CTAs per SM.
-__host__ __device__ inline int npass_class(int D, int nw = kWarps) {
-    const int n = (D + nw * kBinsPerWarp - 1) / (nw * kBinsPerWarp);
-    return n <= 1 ? 1 : n <= 2 ? 2 : n <= 3 ? 3 : n <= 4 ? 4 : 8;
-}
-
 // Forward (detector-gather) evaluation of one work item.  The caller has
 // initialised bar[0..1]; `ph` tracks the barriers' phases so that a
 // persistent CTA can run many items back to back.  Returns false if a
 // bounded wait timed out (copies in flight have been drained).
-template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps>
+// CL > 1: the CTAs of a cluster of CL run the item together, rank r walking
+// lines r, r + CL, ...; every rank returns after the combine, and all of them
+// return false if any rank timed out.
+template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps, int CL = 1>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, DdPhases &ph) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int rank = CL > 1 ? (int)cooperative_groups::this_cluster().block_rank() : 0;
     const int D = g.num_det;
     const DdView2 vw = it.views[v];
     const int xb = vw.xb;
     const int nline = xb ? g.height : g.width;
     const int npix = xb ? g.width : g.height;
     const int rs = rs_entries(npix);
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, WEIGHTED != 0);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, WEIGHTED != 0, CL, NW);
     DdLine *rec = reinterpret_cast<DdLine *>(smem + L.rec);
     DdLine *drec = reinterpret_cast<DdLine *>(smem + L.drec);
     float2 *tab = reinterpret_cast<float2 *>(smem + L.tab);
@@ -316,16 +336,16 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     // the last warp issues the copies: the first warps build the piece
     // constants right after the barrier, on every line's critical path
     const int issuer = (NW - 1) * 32;
-    if (tid == issuer) issue(0, 0);
-    for (int line = 0; line < nline; line++) {
-        const int buf = line & 1;
+    if (tid == issuer && rank < nline) issue(rank, 0);
+    for (int line = rank, step = 0; line < nline; line += CL, step++) {
+        const int buf = step & 1;
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         // past this barrier every warp has finished line - 1, whose buffer
         // takes the copies of line + 1
         __syncthreads();
         if (abort_flag) break;
-        if (tid == issuer && line + 1 < nline) issue(line + 1, buf ^ 1);
+        if (tid == issuer && line + CL < nline) issue(line + CL, buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
         if (WEIGHTED && np > 0) {
@@ -430,7 +450,39 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     // no copy is left in flight here: the next line's copies are issued only
     // after its predecessor's wait succeeded
     __syncthreads();   // the next item's first copies reuse the buffers
-    if (abort_flag) return false;
+    if constexpr (CL > 1) {
+        // ranks > 0 leave their sums in the (idle) line-table space; rank 0
+        // adds them in rank order, so the result does not depend on timing
+        cooperative_groups::cluster_group cluster = cooperative_groups::this_cluster();
+        float *red = reinterpret_cast<float *>(smem + L.tab);
+        if (rank != 0 && !abort_flag) {
+#pragma unroll
+            for (int m = 0; m < kMaxPass; m++) {
+                if (m >= npass) break;
+#pragma unroll
+                for (int b = 0; b < BI; b++) red[(m * BI + b) * (NW * 32) + tid] = acc[m][b];
+            }
+        }
+        cluster.sync();
+        int ab = 0;
+        for (int r = 0; r < CL; r++) ab |= *cluster.map_shared_rank(&abort_flag, r);
+        if (rank == 0 && !ab) {
+            for (int r = 1; r < CL; r++) {
+                const float *rr = cluster.map_shared_rank(red, r);
+#pragma unroll
+                for (int m = 0; m < kMaxPass; m++) {
+                    if (m >= npass) break;
+#pragma unroll
+                    for (int b = 0; b < BI; b++) acc[m][b] += rr[(m * BI + b) * (NW * 32) + tid];
+                }
+            }
+        }
+        cluster.sync();   // no rank leaves (or reuses its buffers) before rank 0 has read them
+        if (ab) return false;
+        if (rank != 0) return true;
+    } else {
+        if (abort_flag) return false;
+    }
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++) {
         if (m >= npass) break;
@@ -439,7 +491,9 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             float beta = 1.0f;
             if (op == DD_OP_PROJ) beta = (GEOM == DD_GEOM_PARA) ? para_beta : it.bcoef[(size_t)v * (D + 1) + k];
             const int ko = vw.flip ? D - 1 - k : k;
-            for (int b = 0; b < nb; b++) {
+#pragma unroll
+            for (int b = 0; b < BI; b++) {   // static indices keep acc in registers
+                if (b >= nb) break;
                 const size_t o = ((size_t)(b0 + b) * it.V + v) * D + ko;
                 // rounded product, then rounded difference: bit-equal to a
                 // separate projection followed by a subtraction (no FMA)
