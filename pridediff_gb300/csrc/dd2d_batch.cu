@@ -244,8 +244,11 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
     }
 }
 
+// Fan beams: held to the plain adjoint's 4 CTAs per SM (64 registers per
+// thread); parallel beams (two sets of accumulators): 3.  The item and its
+// geometry live in shared memory, as in the forward.
 template <int GEOM, int OPK>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, GEOM == DD_GEOM_PARA ? 3 : 4)
 k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ dtabs,
             float *__restrict__ out, const float *__restrict__ base, float scale,
@@ -253,34 +256,41 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
     extern __shared__ __align__(128) unsigned char smem[];
     const AdjSmem SL = adj_smem(GEOM);
     init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
+    __shared__ AdjItem s_it;
+    __shared__ dd_geom2d s_g;
     DdPhases ph;
     for (;;) {
-        const int i = next_item(counter + 1);
+        const int i = next_item(counter + 1);   // its barriers also order s_it's reuse
         if (i >= nitems) break;
-        const int4 w = items[i];
-        const BatchInst &d = desc[w.x];
-        const char *pb = plan + plans_off + d.plan_off;
-        AdjItem it;
-        it.c0 = (w.y & 0xFFFF) * kTile;
-        it.r0 = (w.y >> 16) * kTile;
-        it.b0 = w.z;
-        it.nb = w.w;
-        it.V = d.V;
-        it.nl = d.nl;
-        it.angles = reinterpret_cast<const float *>(pb + d.ang);
-        it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
-        it.dp = reinterpret_cast<const float *>(pb + d.dp);
-        it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
-        it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
-        it.amap = reinterpret_cast<const unsigned char *>(pb + d.amap);
-        it.trange = reinterpret_cast<const int2 *>(pb + d.trange);
-        it.dtab = dtabs + d.dtab_off;
-        it.out = out + d.img_off;
-        it.base = base ? base + d.img_off : nullptr;
-        it.scale = scale;
+        if (threadIdx.x == 0) {
+            const int4 w = items[i];
+            const BatchInst &d = desc[w.x];
+            const char *pb = plan + plans_off + d.plan_off;
+            AdjItem it;
+            it.c0 = (w.y & 0xFFFF) * kTile;
+            it.r0 = (w.y >> 16) * kTile;
+            it.b0 = w.z;
+            it.nb = w.w;
+            it.V = d.V;
+            it.nl = d.nl;
+            it.angles = reinterpret_cast<const float *>(pb + d.ang);
+            it.views = reinterpret_cast<const DdView2 *>(pb + d.views);
+            it.dp = reinterpret_cast<const float *>(pb + d.dp);
+            it.lines = reinterpret_cast<const DdLine *>(pb + d.lines);
+            it.dlines = reinterpret_cast<const DdLine *>(pb + d.dlines);
+            it.amap = reinterpret_cast<const unsigned char *>(pb + d.amap);
+            it.trange = reinterpret_cast<const int2 *>(pb + d.trange);
+            it.dtab = dtabs + d.dtab_off;
+            it.out = out + d.img_off;
+            it.base = base ? base + d.img_off : nullptr;
+            it.scale = scale;
+            s_it = it;
+            s_g = d.g;
+        }
+        __syncthreads();
         bool ok;
-        if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(d.g, it, smem, ph);
-        else ok = adj_tile_map<GEOM, OPK>(d.g, it, smem, ph);
+        if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(s_g, s_it, smem, ph);
+        else ok = adj_tile_map<GEOM, OPK>(s_g, s_it, smem, ph);
         if (!ok) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;

@@ -865,17 +865,24 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
     }
     // merge the two ownerships through shared memory (reusing the record buffers)
     float (*tile)[kTile][kTile + 1] = reinterpret_cast<float (*)[kTile][kTile + 1]>(smem + SL.rec);
-    for (int b = 0; b < nb; b++) {
+    // (b loops unrolled over kBI: static indices keep ax / ay in registers)
+#pragma unroll
+    for (int b = 0; b < kBI; b++) {
+        if (b >= nb) break;
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) tile[b][warp + kWarps * q][lane] = ax[q][b];
     }
     __syncthreads();
-    for (int b = 0; b < nb; b++) {
+#pragma unroll
+    for (int b = 0; b < kBI; b++) {
+        if (b >= nb) break;
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) tile[b][kTile - 1 - lane][warp + kWarps * q] += ay[q][b];
     }
     __syncthreads();
-    for (int b = 0; b < nb; b++) {
+#pragma unroll
+    for (int b = 0; b < kBI; b++) {
+        if (b >= nb) break;
 #pragma unroll
         for (int q = 0; q < kLinesPerWarp; q++) {
             const int r = r0 + warp + kWarps * q, c = c0 + lane;
@@ -1074,7 +1081,9 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     for (int q = 0; q < kLinesPerWarp; q++) {
         const int r = r0 + warp + kWarps * q, c = c0 + lane;
         if (r >= H || c >= W) continue;
-        for (int b = 0; b < nb; b++) {
+#pragma unroll
+        for (int b = 0; b < kBI; b++) {   // static indices keep acc in registers
+            if (b >= nb) break;
             const size_t o = ((size_t)(b0 + b) * H + r) * W + c;
             it.out[o] = it.base ? fmaf(it.scale, acc[q][b], it.base[o]) : acc[q][b];
         }
