@@ -192,18 +192,25 @@ __device__ __forceinline__ int next_item_cluster(int *counter) {
     return i;
 }
 
-// Resident CTAs per SM the persistent forward is compiled for: the plain
-// forward's register budget (40 per thread, 6 CTAs) up to 4 passes.
-__host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <= 4 ? 6 : 3; }
+// Resident CTAs per SM the persistent forward is compiled for (48 registers
+// per thread up to 4 passes; on 24 uneven one-slice instances 5 CTAs per SM
+// ran the forward in 8.13 ms, 6 in 8.20 ms).
+__host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <= 4 ? 5 : 3; }
+
+// CTAs per persistent-forward cluster.  Batches of many short items leave
+// little tail to split: on 24 uneven one-slice instances, clusters of 2 (an
+// item's lines shared as in the single-geometry forward) took 9.00 ms, single
+// CTAs 8.20 ms.
+constexpr int kFwdItemsCluster = 1;
 
 template <int GEOM, int NPASS>
-__global__ void __cluster_dims__(kFwdCluster, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
+__global__ void __cluster_dims__(kFwdItemsCluster, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
 k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
             float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, false, kFwdCluster);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, false, kFwdItemsCluster);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
     // the item and its geometry live in shared memory: read where used, they
     // hold no registers across the line loop (the plain forward reads them
@@ -212,7 +219,9 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
     __shared__ dd_geom2d s_g;
     DdPhases ph;
     for (;;) {
-        const int i = next_item_cluster(counter);
+        int i;
+        if constexpr (kFwdItemsCluster > 1) i = next_item_cluster(counter);
+        else i = next_item(counter);
         if (i >= nitems) break;
         if (threadIdx.x == 0) {
             const int4 w = items[i];
@@ -237,7 +246,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
             s_g = d.g;
         }
         __syncthreads();   // every thread passed the cluster barrier above before s_it changes
-        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
+        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdItemsCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }
@@ -321,8 +330,8 @@ static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
         if ((inst[i].geom.width + kTile - 1) / kTile > 0xFFFF) return DD_ERR_SIZE_OVERFLOW;
         // the persistent forward stages 4 images' line tables per CTA
         const dd_geom2d &g = inst[i].geom;
-        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height)), kBI, false, kFwdCluster)
-                .total > max_smem_optin())
+        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height)), kBI, false,
+                     kFwdItemsCluster).total > max_smem_optin())
             return DD_ERR_SIZE_OVERFLOW;
     }
     return DD_OK;
@@ -367,7 +376,7 @@ template <int GEOM>
 static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
                             float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
-    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, false, kFwdCluster);
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, false, kFwdItemsCluster);
     auto kern = k_fwd_items<GEOM, 8>;
     switch (npass_class(L.Dmax)) {
     case 1: kern = k_fwd_items<GEOM, 1>; break;
@@ -378,7 +387,7 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
     }
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
-    const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, kFwdCluster);
+    const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, kFwdItemsCluster);
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
     kern<<<grid, kThreads, S.total, st>>>(op, (const BatchInst *)(planb + L.desc),
                                           (const int4 *)(planb + L.fitems), L.nfwd, planb, L.plans, tabs,
