@@ -192,6 +192,24 @@ __device__ __forceinline__ void warp_prefix_table(int n, float2 *t, int lane, F 
     }
 }
 
+// FBP weight of a fan-beam pixel centre (px, py) for the source (sx, sy):
+// flat detector r^2 / (r - s.p / r)^2 (FanFlatDisCPU2d.cpp:693, r the
+// source radius), evaluated as (r^2 / (r^2 - s.p))^2 with one correctly
+// rounded reciprocal instead of two divisions; arc detector 1 / |s - p|^2
+// (FanArcDisCPU2d.cpp:703).  Within a few ulp of the reference's FP32
+// sequence; the forward-type and the adjoint-type kernels both use it, so
+// BackProjWeighted and BackProjTransWeighted stay exact transposes.
+template <int GEOM>
+__device__ __forceinline__ float fan_fbp_weight(float sx, float sy, float px, float py, float r) {
+    if (GEOM == DD_GEOM_ARC) {
+        const float a = sx - px, b = sy - py;
+        return __frcp_rn(fmaf(a, a, b * b));
+    }
+    const float r2 = r * r;
+    const float t = r2 * __frcp_rn(r2 - fmaf(sx, px, sy * py));
+    return t * t;
+}
+
 struct Loc {
     int p, j;
     float dl, r;
@@ -274,7 +292,10 @@ struct FwdItem {
 // CL > 1: the CTAs of a cluster of CL run the item together, rank r walking
 // lines r, r + CL, ...; every rank returns after the combine, and all of them
 // return false if any rank timed out.
-template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps, int CL = 1>
+// SPLIT2 (CL == 1): one CTA walks the even lines, then the odd ones, keeping
+// the even lines' sums in its own output elements meanwhile, and adds the
+// two: bit for bit what a 2-CTA cluster computes (out must not alias sub).
+template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps, int CL = 1, bool SPLIT2 = false>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, DdPhases &ph) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
@@ -336,16 +357,38 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     // the last warp issues the copies: the first warps build the piece
     // constants right after the barrier, on every line's critical path
     const int issuer = (NW - 1) * 32;
-    if (tid == issuer && rank < nline) issue(rank, 0);
-    for (int line = rank, step = 0; line < nline; line += CL, step++) {
+    static_assert(!SPLIT2 || CL == 1, "SPLIT2 is the one-CTA form of a 2-CTA cluster");
+    const int nsteps = SPLIT2 ? nline : (rank < nline ? (nline - rank + CL - 1) / CL : 0);
+    const int neven = (nline + 1) / 2;
+    auto line_at = [&](int t) { return SPLIT2 ? (t < neven ? 2 * t : 2 * (t - neven) + 1) : rank + t * CL; };
+    // output element of this thread's accumulator (m, b), -1 if none
+    auto out_slot = [&](int m, int b) -> long long {
+        const int k = m * (NW * kBinsPerWarp) + warp * kBinsPerWarp + lane;
+        if (m >= npass || b >= nb || lane >= kBinsPerWarp || k >= D) return -1;
+        const int ko = vw.flip ? D - 1 - k : k;
+        return ((long long)(b0 + b) * it.V + v) * D + ko;
+    };
+    if (tid == issuer && nsteps > 0) issue(line_at(0), 0);
+    for (int step = 0; step < nsteps; step++) {
+        const int line = line_at(step);
         const int buf = step & 1;
+        if (SPLIT2 && step == neven) {   // even lines done: park their sums
+#pragma unroll
+            for (int m = 0; m < kMaxPass; m++)
+#pragma unroll
+                for (int b = 0; b < BI; b++) {
+                    const long long o = out_slot(m, b);
+                    if (o >= 0) it.out[o] = acc[m][b];
+                    acc[m][b] = 0.0f;
+                }
+        }
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         // past this barrier every warp has finished line - 1, whose buffer
         // takes the copies of line + 1
         __syncthreads();
         if (abort_flag) break;
-        if (tid == issuer && line + CL < nline) issue(line + CL, buf ^ 1);
+        if (tid == issuer && step + 1 < nsteps) issue(line_at(step + 1), buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
         if (WEIGHTED && np > 0) {
@@ -369,8 +412,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                     pcx = lpos;
                     pcy = pix_centre((float)i + 0.5f, g.pix_y, vw.axis0);
                 }
-                ws[i] = (GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
-                                              : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                ws[i] = fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
             }
             float run[BI], inc[BI];
 #pragma unroll
@@ -482,6 +524,15 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         if (rank != 0) return true;
     } else {
         if (abort_flag) return false;
+        if (SPLIT2 && nline > neven) {   // even sums (parked) + odd sums
+#pragma unroll
+            for (int m = 0; m < kMaxPass; m++)
+#pragma unroll
+                for (int b = 0; b < BI; b++) {
+                    const long long o = out_slot(m, b);
+                    if (o >= 0) acc[m][b] = it.out[o] + acc[m][b];
+                }
+        }
     }
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++) {
@@ -775,8 +826,7 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
                     pcx = pix_centre((float)line - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
                     pcy = pix_centre((float)pi + 0.5f, g.pix_y, vw.axis0);
                 }
-                wgt = alpha * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
-                                                     : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
+                wgt = alpha * fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
             }
             if (GEOM == DD_GEOM_PARA) {
                 const DdLine &Ld = drecs[buf * kTile + rel];
@@ -910,7 +960,7 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
 template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
 __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, DdPhases &ph) {
     const AdjSmem SL = adj_smem(GEOM);
-    const int V = it.V, nl = it.nl;
+    const int V = it.V;
     const int W = g.width, H = g.height, D = g.num_det;
     const int rsd = rs_entries(D);
     unsigned char *mapb = smem + SL.map;                           // [kAdjBufs] map blocks
@@ -1036,8 +1086,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
                     pcx = pix_centre((float)line - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
                     pcy = pix_centre((float)pi + 0.5f, g.pix_y, vw.axis0);
                 }
-                wgt = wgt * ((GEOM == DD_GEOM_ARC) ? 1.0f / dd_cw_arc(vw.srcx, vw.srcy, pcx, pcy)
-                                                   : dd_cw_flat(vw.srcx, vw.srcy, pcx, pcy, g.iso_source));
+                wgt = wgt * fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
             }
             const float offU = __int_as_float(up.y), offL = __int_as_float(low.y);
             const bool inU = (unsigned)(up.x - kb) < (unsigned)kn;
