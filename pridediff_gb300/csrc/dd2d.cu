@@ -687,7 +687,6 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
     char *wb = (char *)ws;
     int *status = (int *)(wb + A.status);
     const int geom = geom_of(scan);
-    const int W = g->width, H = g->height;
     if (op_is_forward(op)) {
         float2 *tx = (float2 *)(wb + A.tabx), *ty = (float2 *)(wb + A.taby);
         const int ts = launch_image_tables(g, in, B, tx, ty, st);
