@@ -930,10 +930,12 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
 // Fan-beam adjoint through the adjoint map.  For every view the CTA copies by
 // TMA, for its 32 walked lines, the map entries {bin, offset} of the tile's
 // pixel boundaries, the per-line scales and the slice of every image's
-// detector prefix table the tile can reach.  A thread owns fixed pixels (warp
-// = rows, lane = column) for every view, so one set of accumulators serves
-// both projection axes: pixel value += w (H(upper) - H(lower)), with
-// H(u) = G_k + (u - d_k) g_k read at the two staged boundary entries.
+// detector prefix table the tile can reach.  A thread owns fixed pixels (4
+// consecutive rows of one column: warp = row group, lane = column) for every
+// view, so one set of accumulators serves both projection axes: pixel value
+// += w (H(upper) - H(lower)), with H(u) = G_k + (u - d_k) g_k read at the two
+// staged boundary entries (for views that walk columns the 4 pixels share
+// boundaries: 5 values of H serve them).
 // ---------------------------------------------------------------------------
 template <int GEOM, int OPK>   // OPK: 0 ProjTrans, 1 BackProj, 2 BackProjWeighted
 __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned char *smem, DdPhases &ph) {
@@ -1039,56 +1041,99 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         const float2 *sb = stage + (size_t)buf * kBI * kStage;
         DdView2 vw;   // BackProjWeighted: the view's source and first pixel edge
         if (OPK == 2) vw = it.views[v];
+        // this thread's pixels: rows rq0 .. rq0 + 3 of column c
+        const int rq0 = r0 + kLinesPerWarp * warp, c = c0 + lane;
+        if (!xb) {
+            // views that walk columns: the thread's 4 pixels are consecutive
+            // on its line and pixel q's lower boundary is pixel q + 1's upper
+            // one, so 5 boundary values serve the 4 pixels (the same values:
+            // results are unchanged)
+            const int nv = (c < W) ? min(kLinesPerWarp, H - rq0) : 0;
+            if (nv > 0) {
+                const int lr = c - c0, E = H - rq0 - elo;   // pixel q: upper entry E - q, lower E - q - 1
+                int2 m[kLinesPerWarp + 1];
+                bool all_in = true;   // every used entry in the staged slice (the usual case)
 #pragma unroll
-        for (int q = 0; q < kLinesPerWarp; q++) {
-            const int r = r0 + warp + kWarps * q, c = c0 + lane;
-            if (r >= H || c >= W) continue;
-            int lr, eu;
-            if (xb) {
-                lr = r - r0;
-                eu = c + 1 - elo;
-            } else {
-                lr = c - c0;
-                eu = H - r - elo;
-            }
-            const int2 up = mp[lr * kMapE + eu], low = mp[lr * kMapE + eu - 1];
-            if (up.x < 0 || low.x < 0) continue;
-            float wgt = (OPK == 0) ? 1.0f : alb[lr];
-            if (OPK == 2) {
-                const int line = xb ? r : c, pi = xb ? c : H - 1 - r;
-                float pcx, pcy;
-                if (xb) {
-                    pcx = pix_centre((float)pi + 0.5f, g.pix_x, vw.axis0);
-                    pcy = pix_centre(0.5f * (float)H - (float)line - 0.5f, g.pix_y, g.pix_yshift);
-                } else {
-                    pcx = pix_centre((float)line - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
-                    pcy = pix_centre((float)pi + 0.5f, g.pix_y, vw.axis0);
+                for (int i = 0; i <= kLinesPerWarp; i++) {
+                    m[i] = (i <= nv) ? mp[lr * kMapE + E - i] : make_int2(-1, 0);
+                    if (m[i].x >= 0 && (unsigned)(m[i].x - kb) >= (unsigned)kn) all_in = false;
                 }
-                wgt = wgt * fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
-            }
-            const float offU = __int_as_float(up.y), offL = __int_as_float(low.y);
-            const bool inU = (unsigned)(up.x - kb) < (unsigned)kn;
-            const bool inL = (unsigned)(low.x - kb) < (unsigned)kn;
-            if (inU && inL) {   // both entries in the staged slice (the usual case)
-                const float2 *su = sb + (up.x - kb), *sl = sb + (low.x - kb);
+                float wq[kLinesPerWarp];
 #pragma unroll
-                for (int b = 0; b < kBI; b++) {
-                    if (b >= nb) break;
-                    const float2 e = su[b * kStage], e2 = sl[b * kStage];
-                    const float hu = fmaf(offU, e.y, e.x);
-                    const float hl = fmaf(offL, e2.y, e2.x);
-                    acc[q][b] += wgt * (hu - hl);
+                for (int q = 0; q < kLinesPerWarp; q++) {
+                    float wgt = (OPK == 0) ? 1.0f : alb[lr];
+                    if (OPK == 2) {
+                        const float pcx = pix_centre((float)c - 0.5f * (float)W + 0.5f, g.pix_x, g.pix_xshift);
+                        const float pcy = pix_centre((float)(H - 1 - (rq0 + q)) + 0.5f, g.pix_y, vw.axis0);
+                        wgt = wgt * fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                    }
+                    wq[q] = wgt;
                 }
-            } else {
 #pragma unroll
                 for (int b = 0; b < kBI; b++) {
                     if (b >= nb) break;
                     const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
-                    const float2 e = inU ? sb[b * kStage + (up.x - kb)] : __ldg(t + up.x);
-                    const float2 e2 = inL ? sb[b * kStage + (low.x - kb)] : __ldg(t + low.x);
-                    const float hu = fmaf(offU, e.y, e.x);
-                    const float hl = fmaf(offL, e2.y, e2.x);
-                    acc[q][b] += wgt * (hu - hl);
+                    float h[kLinesPerWarp + 1];
+                    if (all_in) {
+#pragma unroll
+                        for (int i = 0; i <= kLinesPerWarp; i++) {
+                            const float2 e = sb[b * kStage + max(m[i].x - kb, 0)];
+                            h[i] = fmaf(__int_as_float(m[i].y), e.y, e.x);   // unused where m[i].x < 0
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i <= kLinesPerWarp; i++) {
+                            h[i] = 0.0f;
+                            if (m[i].x >= 0) {
+                                const bool in = (unsigned)(m[i].x - kb) < (unsigned)kn;
+                                const float2 e = in ? sb[b * kStage + (m[i].x - kb)] : __ldg(t + m[i].x);
+                                h[i] = fmaf(__int_as_float(m[i].y), e.y, e.x);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < kLinesPerWarp; q++)
+                        if (q < nv && m[q].x >= 0 && m[q + 1].x >= 0) acc[q][b] += wq[q] * (h[q] - h[q + 1]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < kLinesPerWarp; q++) {
+                const int r = rq0 + q;
+                if (r >= H || c >= W) continue;
+                const int lr = r - r0, eu = c + 1 - elo;   // line r, pixel c
+                const int2 up = mp[lr * kMapE + eu], low = mp[lr * kMapE + eu - 1];
+                if (up.x < 0 || low.x < 0) continue;
+                float wgt = (OPK == 0) ? 1.0f : alb[lr];
+                if (OPK == 2) {
+                    const float pcx = pix_centre((float)c + 0.5f, g.pix_x, vw.axis0);
+                    const float pcy = pix_centre(0.5f * (float)H - (float)r - 0.5f, g.pix_y, g.pix_yshift);
+                    wgt = wgt * fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pcx, pcy, g.iso_source);
+                }
+                const float offU = __int_as_float(up.y), offL = __int_as_float(low.y);
+                const bool inU = (unsigned)(up.x - kb) < (unsigned)kn;
+                const bool inL = (unsigned)(low.x - kb) < (unsigned)kn;
+                if (inU && inL) {   // both entries in the staged slice (the usual case)
+                    const float2 *su = sb + (up.x - kb), *sl = sb + (low.x - kb);
+#pragma unroll
+                    for (int b = 0; b < kBI; b++) {
+                        if (b >= nb) break;
+                        const float2 e = su[b * kStage], e2 = sl[b * kStage];
+                        const float hu = fmaf(offU, e.y, e.x);
+                        const float hl = fmaf(offL, e2.y, e2.x);
+                        acc[q][b] += wgt * (hu - hl);
+                    }
+                } else {
+#pragma unroll
+                    for (int b = 0; b < kBI; b++) {
+                        if (b >= nb) break;
+                        const float2 *t = dtab + ((size_t)(b0 + b) * V + v) * rsd;   // per image
+                        const float2 e = inU ? sb[b * kStage + (up.x - kb)] : __ldg(t + up.x);
+                        const float2 e2 = inL ? sb[b * kStage + (low.x - kb)] : __ldg(t + low.x);
+                        const float hu = fmaf(offU, e.y, e.x);
+                        const float hl = fmaf(offL, e2.y, e2.x);
+                        acc[q][b] += wgt * (hu - hl);
+                    }
                 }
             }
         }
@@ -1106,7 +1151,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
     }
 #pragma unroll
     for (int q = 0; q < kLinesPerWarp; q++) {
-        const int r = r0 + warp + kWarps * q, c = c0 + lane;
+        const int r = r0 + kLinesPerWarp * warp + q, c = c0 + lane;
         if (r >= H || c >= W) continue;
 #pragma unroll
         for (int b = 0; b < kBI; b++) {   // static indices keep acc in registers
