@@ -200,8 +200,10 @@ __host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <
 // CTAs per persistent-forward cluster.  Batches of many short items leave
 // little tail to split: on 24 uneven one-slice instances, clusters of 2 (an
 // item's lines shared as in the single-geometry forward) took 9.00 ms, single
-// CTAs 8.20 ms.  A single CTA sums the lines in the cluster's order (SPLIT2),
-// so an instance's projection is bit-equal to the single-geometry one.
+// CTAs 8.20 ms.  A single CTA sums a view's lines in one sequence, the
+// single-geometry forward's cluster as two interleaved halves, so the two
+// projections of an instance agree to FP32 rounding, not bit for bit
+// (walking the lines in the cluster's order cost 8.73 vs 8.13 ms).
 constexpr int kFwdItemsCluster = 1;
 
 template <int GEOM, int NPASS>
@@ -247,9 +249,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
             s_g = d.g;
         }
         __syncthreads();   // every thread passed the cluster barrier above before s_it changes
-        // out is the caller's sinogram or the workspace residual, never y (sub)
-        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdItemsCluster, kFwdItemsCluster == 1 && kFwdCluster == 2>(
-                s_g, op, s_it, smem, Dmax, rsmax, ph)) {
+        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdItemsCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
             break;
         }

@@ -291,10 +291,7 @@ struct FwdItem {
 // CL > 1: the CTAs of a cluster of CL run the item together, rank r walking
 // lines r, r + CL, ...; every rank returns after the combine, and all of them
 // return false if any rank timed out.
-// SPLIT2 (CL == 1): one CTA walks the even lines, then the odd ones, keeping
-// the even lines' sums in its own output elements meanwhile, and adds the
-// two: bit for bit what a 2-CTA cluster computes (out must not alias sub).
-template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps, int CL = 1, bool SPLIT2 = false>
+template <int GEOM, int WEIGHTED, int NPASS, int BI = kBI, int NW = kWarps, int CL = 1>
 __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned char *smem,
                          int Dmax, int rsmax, DdPhases &ph) {
     const int v = it.v, b0 = it.b0, nb = it.nb;
@@ -355,38 +352,16 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     // the last warp issues the copies: the first warps build the piece
     // constants right after the barrier, on every line's critical path
     const int issuer = (NW - 1) * 32;
-    static_assert(!SPLIT2 || CL == 1, "SPLIT2 is the one-CTA form of a 2-CTA cluster");
-    const int nsteps = SPLIT2 ? nline : (rank < nline ? (nline - rank + CL - 1) / CL : 0);
-    const int neven = (nline + 1) / 2;
-    auto line_at = [&](int t) { return SPLIT2 ? (t < neven ? 2 * t : 2 * (t - neven) + 1) : rank + t * CL; };
-    // output element of this thread's accumulator (m, b), -1 if none
-    auto out_slot = [&](int m, int b) -> long long {
-        const int k = m * (NW * kBinsPerWarp) + warp * kBinsPerWarp + lane;
-        if (m >= npass || b >= nb || lane >= kBinsPerWarp || k >= D) return -1;
-        const int ko = vw.flip ? D - 1 - k : k;
-        return ((long long)(b0 + b) * it.V + v) * D + ko;
-    };
-    if (tid == issuer && nsteps > 0) issue(line_at(0), 0);
-    for (int step = 0; step < nsteps; step++) {
-        const int line = line_at(step);
+    if (tid == issuer && rank < nline) issue(rank, 0);
+    for (int line = rank, step = 0; line < nline; line += CL, step++) {
         const int buf = step & 1;
-        if (SPLIT2 && step == neven) {   // even lines done: park their sums
-#pragma unroll
-            for (int m = 0; m < kMaxPass; m++)
-#pragma unroll
-                for (int b = 0; b < BI; b++) {
-                    const long long o = out_slot(m, b);
-                    if (o >= 0) it.out[o] = acc[m][b];
-                    acc[m][b] = 0.0f;
-                }
-        }
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         // past this barrier every warp has finished line - 1, whose buffer
         // takes the copies of line + 1
         __syncthreads();
         if (abort_flag) break;
-        if (tid == issuer && step + 1 < nsteps) issue(line_at(step + 1), buf ^ 1);
+        if (tid == issuer && line + CL < nline) issue(line + CL, buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
         if (WEIGHTED && np > 0) {
@@ -502,15 +477,6 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         if (rank != 0) return true;
     } else {
         if (abort_flag) return false;
-        if (SPLIT2 && nline > neven) {   // even sums (parked) + odd sums
-#pragma unroll
-            for (int m = 0; m < kMaxPass; m++)
-#pragma unroll
-                for (int b = 0; b < BI; b++) {
-                    const long long o = out_slot(m, b);
-                    if (o >= 0) acc[m][b] = it.out[o] + acc[m][b];
-                }
-        }
     }
 #pragma unroll
     for (int m = 0; m < kMaxPass; m++) {

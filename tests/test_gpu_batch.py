@@ -41,8 +41,11 @@ def test_batched_forward_and_adjoint_equal_per_instance(scan):
     ub = UnevenBatch2d(projs, angs, batch)
     xs = _rand_images(projs, batch, 2)
     ys = ub.unpack_sinos(ub.forward(ub.pack(xs)))
+    # the single-geometry forward sums a view's lines as two interleaved
+    # halves (one per CTA of a cluster), the persistent one in one sequence:
+    # FP32 rounding apart; the adjoints are the same computation, bit for bit
     for p, a, x, y in zip(projs, angs, xs, ys):
-        assert torch.equal(y, p.projection(x, a))
+        assert rel_l2(y.cpu().numpy(), p.projection(x, a).cpu().numpy()) <= 1e-6
     g = torch.Generator(device="cuda").manual_seed(3)
     rs = [torch.randn(s, device="cuda", generator=g) for s in ub.sino_shapes]
     bs = ub.unpack_images(ub.adjoint(ub.pack(rs)))
