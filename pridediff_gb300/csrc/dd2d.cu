@@ -98,13 +98,7 @@ __global__ void k_tab_cols(const float *__restrict__ img, int B, int H, int W,
     const int b = idx / W, col = idx - b * W;
     const float *im = img + (size_t)b * H * W;
     float2 *t = tab + (size_t)idx * rs_entries(H);
-    DdF run = {0.0f, 0.0f};
-    for (int i = 0; i < H; i++) {
-        const float x = im[(size_t)(H - 1 - i) * W + col];
-        t[i] = make_float2(run.hi, x);
-        run = df_add(run, DdF{x, 0.0f});
-    }
-    t[H] = make_float2(run.hi, 0.0f);
+    col_prefix_table(im, H, W, col, t);
 }
 
 // Detector tables for the adjoint: per (image, view) G_k and g_k over the

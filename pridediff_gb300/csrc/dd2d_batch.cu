@@ -130,13 +130,7 @@ __global__ void k_tab_cols_b(const BatchInst *__restrict__ desc, const float *__
     const int b = idx / W, col = idx - b * W;
     const float *im = img + d.img_off + (size_t)b * H * W;
     float2 *t = tabs + d.taby_off + (size_t)idx * rs_entries(H);
-    DdF run = {0.0f, 0.0f};
-    for (int i = 0; i < H; i++) {
-        const float x = im[(size_t)(H - 1 - i) * W + col];
-        t[i] = make_float2(run.hi, x);
-        run = df_add(run, DdF{x, 0.0f});
-    }
-    t[H] = make_float2(run.hi, 0.0f);
+    col_prefix_table(im, H, W, col, t);
 }
 
 __global__ void k_dettab_b(int geom, int mode, const BatchInst *__restrict__ desc,
