@@ -52,8 +52,8 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // moved by a single bulk copy: dp (C+1 column boundaries), mag (C column
 // magnifications), rowz (R x {row0z, row1z}).
 struct PlanLayout {
-    size_t views, dp, mag, rowz, linez, lines, total;
-    int nl, nch, sdp, smag, srz;
+    size_t views, dp, mag, rowz, linez, lines, slabv, total;
+    int nl, nch, sdp, smag, srz, nslab;
 };
 
 __host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
@@ -73,6 +73,8 @@ inline PlanLayout plan_layout(const dd_geom3d *g, int V) {
     L.rowz = o; o = align_up(o + sizeof(float) * (size_t)V * L.srz, 256);
     L.linez = o; o = align_up(o + sizeof(float4) * (size_t)V * L.nl, 256);
     L.lines = o; o = align_up(o + sizeof(DdLine) * (size_t)V * L.nl * L.nch, 256);
+    L.nslab = (g->depth + kZS - 1) / kZS;   // the adjoint's slabs of kZS slices
+    L.slabv = o; o = align_up(o + sizeof(int2) * (size_t)L.nslab, 256);
     L.total = o;
     return L;
 }
@@ -507,6 +509,39 @@ __device__ __forceinline__ bool slab_visible(const dd_geom3d &g, const DdView3 &
     return dd3_slab_lit(&w, fminf(m0, m1), fmaxf(m0, m1), zsA, zsB, zr0, zr1);
 }
 
+// Plan time: for each slab of kZS slices, the views [first, last] whose
+// detector can see it anywhere in the image -- slab_visible over the whole
+// image's lines, a superset of what it admits for any tile's lines (wider
+// magnification bounds only widen the lit band) -- stored as {first,
+// last + 1}, {0, 0} if none.  The adjoint loops over these views only: on a
+// spiral a slab is lit during one pass of the helix.
+__global__ void __launch_bounds__(256) k_slab_views3(dd_geom3d g, char *plan, PlanLayout P, int V) {
+    const int slab = blockIdx.x, R = g.num_row;
+    const DdView3 *views = reinterpret_cast<const DdView3 *>(plan + P.views);
+    const float *rzt = reinterpret_cast<const float *>(plan + P.rowz);
+    __shared__ int lo, hi;
+    if (threadIdx.x == 0) {
+        lo = V;
+        hi = -1;
+    }
+    __syncthreads();
+    int mylo = V, myhi = -1;
+    for (int v = threadIdx.x; v < V; v += blockDim.x) {
+        const DdView3 w = views[v];
+        const int nline = w.xb ? g.height : g.width;
+        const float *rzv = rzt + (size_t)v * P.srz;
+        if (slab_visible(g, w, 0, nline - 1, slab * kZS, rzv[0], rzv[2 * R - 1])) {
+            mylo = min(mylo, v);
+            myhi = max(myhi, v);
+        }
+    }
+    atomicMin(&lo, mylo);
+    atomicMax(&hi, myhi);
+    __syncthreads();
+    if (threadIdx.x == 0)
+        reinterpret_cast<int2 *>(plan + P.slabv)[slab] = hi >= lo ? make_int2(lo, hi + 1) : make_int2(0, 0);
+}
+
 // grid: (voxel-column tile, slab of kZS slices, volume group); thread = one
 // (x, y) voxel column of a 16 x 16 tile.  Views whose detector cannot see the
 // slab are skipped when their copy would be issued.
@@ -574,15 +609,17 @@ __global__ void __launch_bounds__(kThreads, 3) k_adj3(const Adj3Args a) {
 
     DdPhases ph;
     int inflight = -1;
-    if (tid == 0) issue(0, 0);
-    for (int v = 0; v < a.V; v++) {
-        const int buf = v & 1;
-        if (tid == 0 && v + 1 < a.V) issue(v + 1, buf ^ 1);
+    // only the views that can see this slab somewhere in the image
+    const int2 vr = reinterpret_cast<const int2 *>(a.plan + P.slabv)[blockIdx.y];
+    if (tid == 0 && vr.x < vr.y) issue(vr.x, 0);
+    for (int v = vr.x; v < vr.y; v++) {
+        const int buf = (v - vr.x) & 1;
+        if (tid == 0 && v + 1 < vr.y) issue(v + 1, buf ^ 1);
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         __syncthreads();
         if (abort_flag) {
-            inflight = (v + 1 < a.V) ? (buf ^ 1) : -1;
+            inflight = (v + 1 < vr.y) ? (buf ^ 1) : -1;
             break;
         }
         if (active && seen[buf]) {
@@ -726,8 +763,9 @@ int plan(int scan, const dd_geom3d *g, const float *angles, const float *sp, int
         k_views3<DD_GEOM3_SPIRAL><<<V, kThreads, 0, st>>>(*g, angles, sp, V, base, P);
         k_lines3<DD_GEOM3_SPIRAL><<<gl, 128, 0, st>>>(*g, base, P);
     }
+    k_slab_views3<<<P.nslab, 256, 0, st>>>(*g, base, P, V);
     dd2::prof_end(pr, st);
-    dd2::count_launches(2);
+    dd2::count_launches(3);
     return launch_status();
 }
 
