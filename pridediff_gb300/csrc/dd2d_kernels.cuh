@@ -396,25 +396,37 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
             // BackProjTransWeighted: multiply every pixel by its FBP weight at
             // this view (FanFlatDisCPU2d.cpp:693, FanArcDisCPU2d.cpp:703) and
             // rebuild the line's prefix table in place: warp b scans image b
-            // in 32-pixel chunks (weights in registers, conflict-free
-            // accesses), then builds that image's piece constants below, so
-            // the rebuild needs no CTA barrier.  (Two warps per image, 4
-            // pixels per lane, were slower: 12.4 vs 11.3 ms for 16 slices.)
+            // in 128-pixel chunks (4 consecutive pixels per lane, weights in
+            // registers), then builds that image's piece constants below, so
+            // the rebuild needs no CTA barrier.
             if (warp < nb) {
                 float2 *t = tab + ((size_t)buf * BI + warp) * rsmax;
                 const float lpos = xb
                     ? pix_centre(0.5f * (float)g.height - (float)line - 0.5f, g.pix_y, g.pix_yshift)
                     : pix_centre((float)line - 0.5f * (float)g.width + 0.5f, g.pix_x, g.pix_xshift);
+                const float pitch = xb ? g.pix_x : g.pix_y;
                 float carry = 0.0f;
-                for (int k0 = 0; k0 < npix; k0 += 32) {
-                    const int i = k0 + lane;
-                    float y = 0.0f;
-                    if (i < npix) {
-                        const float pc = pix_centre((float)i + 0.5f, xb ? g.pix_x : g.pix_y, vw.axis0);
-                        y = t[i].y * (xb ? fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pc, lpos, g.iso_source)
-                                         : fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, lpos, pc, g.iso_source));
+                // 128-pixel chunks, 4 consecutive pixels per lane (two 16-byte
+                // loads; rows are 16-byte aligned and rsmax is even)
+                for (int k0 = 0; k0 < npix; k0 += 128) {
+                    const int i0 = k0 + 4 * lane;
+                    float y[4];
+                    if (i0 + 3 < npix) {
+                        const float4 p01 = *reinterpret_cast<const float4 *>(t + i0);
+                        const float4 p23 = *reinterpret_cast<const float4 *>(t + i0 + 2);
+                        y[0] = p01.y; y[1] = p01.w; y[2] = p23.y; y[3] = p23.w;
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; e++) y[e] = (i0 + e < npix) ? t[i0 + e].y : 0.0f;
                     }
-                    float inc = y;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float pc = pix_centre((float)(i0 + e) + 0.5f, pitch, vw.axis0);
+                        y[e] *= xb ? fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, pc, lpos, g.iso_source)
+                                   : fan_fbp_weight<GEOM>(vw.srcx, vw.srcy, lpos, pc, g.iso_source);
+                    }
+                    const float r1 = y[0] + y[1], r2 = r1 + y[2], r3 = r2 + y[3];
+                    float inc = r3;
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) {
                         const float z = __shfl_up_sync(0xffffffffu, inc, o);
@@ -422,7 +434,16 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
                     }
                     float prev = __shfl_up_sync(0xffffffffu, inc, 1);
                     if (lane == 0) prev = 0.0f;
-                    if (i < npix) t[i] = make_float2(carry + prev, y);
+                    const float base = carry + prev;
+                    const float pre[4] = {base, base + y[0], base + r1, base + r2};
+                    if (i0 + 3 < npix) {
+                        *reinterpret_cast<float4 *>(t + i0) = make_float4(pre[0], y[0], pre[1], y[1]);
+                        *reinterpret_cast<float4 *>(t + i0 + 2) = make_float4(pre[2], y[2], pre[3], y[3]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if (i0 + e < npix) t[i0 + e] = make_float2(pre[e], y[e]);
+                    }
                     carry += __shfl_sync(0xffffffffu, inc, 31);
                 }
                 if (lane == 0) t[npix] = make_float2(carry, 0.0f);
