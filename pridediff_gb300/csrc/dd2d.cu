@@ -149,7 +149,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, WEIGHTED != 0, kFwdCluster, NW);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, kFwdCluster, NW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     DdPhases ph;
@@ -571,9 +571,9 @@ static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const cha
     // 4 images per CTA; 2 where the line tables of 4 would not fit in shared
     // memory (lines of more than about 3,400 pixels)
     constexpr int NW = kFwdWarps;
-    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, w, kFwdCluster, NW).total <= max_smem_optin()
+    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, kFwdCluster, NW).total <= max_smem_optin()
                        ? kFwdImages : 2;
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, w, kFwdCluster, NW);
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, kFwdCluster, NW);
     if (S.total > max_smem_optin()) return DD_ERR_SIZE_OVERFLOW;
     if ((long long)V * kFwdCluster > 0x7FFFFFFFLL) return DD_ERR_SIZE_OVERFLOW;
     dim3 grid(V * kFwdCluster, (B + bi - 1) / bi);

@@ -207,7 +207,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
             float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, false, kFwdItemsCluster);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, kFwdItemsCluster);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
     // the item and its geometry live in shared memory: read where used, they
     // hold no registers across the line loop (the plain forward reads them
@@ -327,7 +327,7 @@ static int validate_batch(int scan, int op, const dd_instance2d *inst, int n) {
         if ((inst[i].geom.width + kTile - 1) / kTile > 0xFFFF) return DD_ERR_SIZE_OVERFLOW;
         // the persistent forward stages 4 images' line tables per CTA
         const dd_geom2d &g = inst[i].geom;
-        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height)), kBI, false,
+        if (fwd_smem(geom_of(scan), g.num_det, rs_entries(std::max(g.width, g.height)), kBI,
                      kFwdItemsCluster).total > max_smem_optin())
             return DD_ERR_SIZE_OVERFLOW;
     }
@@ -373,7 +373,7 @@ template <int GEOM>
 static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
                             float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
-    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, false, kFwdItemsCluster);
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, kFwdItemsCluster);
     auto kern = k_fwd_items<GEOM, 8>;
     switch (npass_class(L.Dmax)) {
     case 1: kern = k_fwd_items<GEOM, 1>; break;

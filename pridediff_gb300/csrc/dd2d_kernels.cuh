@@ -277,11 +277,11 @@ struct FwdSmem {
 // distributed shared memory.
 constexpr int kFwdCluster = 2;
 
-// weighted: BackProjTransWeighted (same layout: its weights live in registers).
+// (BackProjTransWeighted uses the same layout: its weights live in registers.)
 // cl > 1: the line tables' space also holds a CTA's sums for the combine
 // (npass_class(D) passes x bi images x 32 lanes x nw warps floats).
-__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI, bool weighted = false,
-                                            int cl = 1, int nw = kWarps) {
+__host__ __device__ inline FwdSmem fwd_smem(int geom, int D, int rsmax, int bi = kBI, int cl = 1,
+                                            int nw = kWarps) {
     FwdSmem s;
     int o = 0;
     s.rec = o; o += 2 * (int)sizeof(DdLine);
@@ -331,7 +331,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
     const int nline = xb ? g.height : g.width;
     const int npix = xb ? g.width : g.height;
     const int rs = rs_entries(npix);
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, WEIGHTED != 0, CL, NW);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, CL, NW);
     DdLine *rec = reinterpret_cast<DdLine *>(smem + L.rec);
     DdLine *drec = reinterpret_cast<DdLine *>(smem + L.drec);
     float2 *tab = reinterpret_cast<float2 *>(smem + L.tab);
