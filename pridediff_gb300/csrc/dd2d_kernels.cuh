@@ -196,19 +196,20 @@ __device__ __forceinline__ void warp_prefix_table(int n, float2 *t, int lane, F 
 
 // FBP weight of a fan-beam pixel centre (px, py) for the source (sx, sy):
 // flat detector r^2 / (r - s.p / r)^2 (FanFlatDisCPU2d.cpp:693, r the
-// source radius), evaluated as (r^2 / (r^2 - s.p))^2 with one correctly
-// rounded reciprocal instead of two divisions; arc detector 1 / |s - p|^2
-// (FanArcDisCPU2d.cpp:703).  Within a few ulp of the reference's FP32
-// sequence; the forward-type and the adjoint-type kernels both use it, so
-// BackProjWeighted and BackProjTransWeighted stay exact transposes.
+// source radius), evaluated as (r^2 / (r^2 - s.p))^2 with one fast division
+// (__fdividef: within 2 ulp for these magnitudes) instead of two IEEE
+// divisions; arc detector 1 / |s - p|^2 (FanArcDisCPU2d.cpp:703).  Within a
+// few ulp of the reference's FP32 sequence; the forward-type and the
+// adjoint-type kernels both use it, so BackProjWeighted and
+// BackProjTransWeighted stay exact transposes.
 template <int GEOM>
 __device__ __forceinline__ float fan_fbp_weight(float sx, float sy, float px, float py, float r) {
     if (GEOM == DD_GEOM_ARC) {
         const float a = sx - px, b = sy - py;
-        return __frcp_rn(fmaf(a, a, b * b));
+        return __fdividef(1.0f, fmaf(a, a, b * b));
     }
     const float r2 = r * r;
-    const float t = r2 * __frcp_rn(r2 - fmaf(sx, px, sy * py));
+    const float t = __fdividef(r2, r2 - fmaf(sx, px, sy * py));
     return t * t;
 }
 
