@@ -14,7 +14,8 @@ Metric: FP+BP per second (slice forward + adjoint pairs per second).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
 
 On one GPU the line also carries `extra`: the same slices through the plain
-per-slice path (the unbatched comparator), the FBP of the 16 sinograms (fused
+per-slice path (the unbatched comparator), the parallel-beam configuration
+(one 256^2 slice, 180 views, 367 detectors), the FBP of the 16 sinograms (fused
 weight + filter kernel, then the weighted back-projection, beside the
 reference's torch-convolution composition), the 24-instance uneven batched
 data-consistency loop captured in a CUDA graph, and the 3-D cone-flat and
@@ -252,6 +253,28 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
                                   "ms_per_step": ms, "value": B / (ms / 1e3), "unit": UNIT}
     except Exception as e:   # report, never hide the headline line
         out["plain_per_slice"] = {"error": repr(e)}
+
+    # parallel beam, the reference's CPU-runnable configuration: one 256^2 slice
+    # at 1 mm, 180 views over 180 degrees, 367 detectors of 1 mm; loss + backward
+    try:
+        projp = P.projector2d(256, 367, 1.0, 1.0, 500.0, 1000.0, scan_type="para").to(dev)
+        angp = torch.arange(180, dtype=torch.float32, device=dev) * (np.pi / 180)
+        xp = torch.from_numpy(phantom(256, 256, 10, np.random.default_rng(7), 1.0))[None, None].to(dev)
+        with torch.no_grad():
+            yp = projp.projection(xp, angp)
+
+        def stepp():
+            xr = (xp * 0.8).requires_grad_(True)
+            ((projp.projection(xr, angp) - yp) ** 2).sum().backward()
+        ms = _timed(stepp, 20, flush, ev)
+        nbp = 2 * 4.0 * 180 * (256 * 256 + 367)
+        out["para_1x256_180v"] = {"what": "parallel beam 256^2 at 1 mm, 180 views over 180 deg, 367 dets of 1 mm, "
+                                          "one slice, loss + backward (launch-latency bound)",
+                                  "ms_per_step": ms, "value": 1 / (ms / 1e3), "unit": UNIT, **frac(nbp, ms),
+                                  "bytes_model": "view-swept 4*V*(H*W + D) per slice and operator"}
+        del projp, xp, yp
+    except Exception as e:   # report, never hide the headline line
+        out["para_1x256_180v"] = {"error": repr(e)}
 
     # FBP (deeprecon's filtered_backprojection) of the headline sinograms
     try:
