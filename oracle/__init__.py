@@ -89,6 +89,15 @@ def _load():
             f3.argtypes = [ctypes.POINTER(_Geom3), ctypes.c_int, ctypes.c_int,
                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                            ctypes.POINTER(ct), ctypes.POINTER(ct), ctypes.c_int, ctypes.c_int]
+        lib.ddo_f_ddo_scan2d.restype = ctypes.c_longlong
+        lib.ddo_f_ddo_scan2d.argtypes = [ctypes.POINTER(_Geom2), ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_float), ctypes.c_double,
+                                         ctypes.POINTER(ctypes.c_int)]
+        lib.ddo_f_ddo_scan3d.restype = ctypes.c_longlong
+        lib.ddo_f_ddo_scan3d.argtypes = [ctypes.POINTER(_Geom3), ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(ctypes.c_float), ctypes.c_double,
+                                         ctypes.POINTER(ctypes.c_int)]
         lib.ddo_default_threads.restype = ctypes.c_int
         lib.ddo_default_threads.argtypes = [ctypes.c_int]
         _lib = lib
@@ -189,6 +198,43 @@ def run3d(geom: str, op: str, x: np.ndarray, angles: np.ndarray, options,
     if rc != 0:
         raise ValueError(f"oracle run3d rejected geom={geom} op={op}")
     return out
+
+
+# margin of the start-index scan, in detector cells / pixels: some 20 to 50
+# times the few-ulp differences between this FP32 restatement and the device
+# code (fused multiply-adds, its own tan / atan), far below one cell
+SCAN_MARGIN = 1e-3
+
+
+def scan_hazards(geom: str, angles: np.ndarray, options, source_pos: np.ndarray | None = None,
+                 margin: float = SCAN_MARGIN) -> np.ndarray:
+    """Walk starts of deeprecon's CUDA kernels that could round to index -1.
+
+    Returns, per view, how many (256-column block, image line) starts of the
+    reference kernels lie within ``margin`` of a negative detector or pixel
+    index on this geometry (ddoracle_body.h, ``ddo_scan2d`` / ``ddo_scan3d``).
+    Only views with 0 are run on the reference kernels (``safe_views``)."""
+    lib = _load()
+    ang = np.ascontiguousarray(angles, dtype=np.float32)
+    per = np.zeros(ang.size, np.int32)
+    pv = _ptr(per, ctypes.c_int)
+    if geom in GEOM2:
+        g = geom2_from_options(options, ang.size)
+        lib.ddo_f_ddo_scan2d(ctypes.byref(g), GEOM2[geom], _ptr(ang, ctypes.c_float), float(margin), pv)
+        return per
+    g = geom3_from_options(options, ang.size, spiral=(geom == "spiral"))
+    sp = None if source_pos is None else np.ascontiguousarray(source_pos, dtype=np.float32)
+    n = lib.ddo_f_ddo_scan3d(ctypes.byref(g), GEOM3[geom], _ptr(ang, ctypes.c_float),
+                             _ptr(sp, ctypes.c_float) if sp is not None else None, float(margin), pv)
+    if n < 0:
+        raise ValueError("spiral scan needs source_pos")
+    return per
+
+
+def safe_views(geom: str, angles: np.ndarray, options, source_pos: np.ndarray | None = None) -> np.ndarray:
+    """Indices of the views on which deeprecon's CUDA kernels start every walk
+    at least ``SCAN_MARGIN`` away from a negative index."""
+    return np.flatnonzero(scan_hazards(geom, angles, options, source_pos) == 0)
 
 
 _REF_NAMES = {

@@ -64,6 +64,15 @@ int ddo_d_ddo_run3d(const ddo_geom3 *g, int geom, int op, const float *angles,
                     const float *source_pos, const double *in, double *out, int batch,
                     int nthreads);
 
+/* Start-index scan of deeprecon's CUDA kernels (see ddoracle_body.h): the
+ * number of (view, 256-column block, line) walk starts whose detector or
+ * pixel index lies within `margin` of rounding to -1.  0 means the case is
+ * safe to run on the reference kernels. */
+long long ddo_f_ddo_scan2d(const ddo_geom2 *g, int geom, const float *angles, double margin,
+                           int *per_view);
+long long ddo_f_ddo_scan3d(const ddo_geom3 *g, int geom, const float *angles,
+                           const float *source_pos, double margin, int *per_view);
+
 #ifdef __cplusplus
 }
 #endif

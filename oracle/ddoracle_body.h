@@ -677,3 +677,158 @@ int FN(ddo_run3d)(const ddo_geom3 *g, int geom, int op, const float *angles,
     for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Start-index scan of deeprecon's CUDA kernels                             */
+/* ------------------------------------------------------------------------ */
+
+/* deeprecon's CUDA kernels start the walk of each (view, block of 256
+ * detector columns, image line) at a detector index and a pixel index taken
+ * from two different formulas: the flat-detector kernels map the line's first
+ * pixel boundary back onto the detector (FanFlatDisCUDA2d.cu:96-104,
+ * ConeFlatDisCUDA3d.cu:116-127), the arc ones compare angles through atan
+ * and then locate the block's first column among the pixels
+ * (FanArcDisCUDA2d.cu:97-110, ConeArcDisCUDA3d.cu:84-96, SpiralDisCUDA3d.cu:93-105).
+ * Both are >= 0 in exact arithmetic, but where the image edge and the
+ * block's first column boundary coincide to within rounding one of them can
+ * floor to -1, and the kernel then indexes shared memory (ProjTemp[-1]) or
+ * its output (atomicAdd at column -1) out of bounds.  The scan evaluates
+ * those start values for every (view, block, line) with the reference's FP32
+ * arithmetic and counts the starts that lie within `margin` (in detector
+ * cells or pixels; ten times that for the arc kernels' angle-based detector
+ * index, whose atan/tan chain rounds more loosely) of such a rounding,
+ * taking either branch of a start decision whose two operands tie to within
+ * 2e-6 relative (17 to 33 FP32 ulps: the device code's fused multiply-adds
+ * and its own tan/atan move them by a few).  `per_view` (optional, nv
+ * entries) receives the count of each view, so that a case can be run on the
+ * views without any.  A case with count 0 can be given to
+ * the reference kernels; one with a non-zero count is not run there.  The
+ * parallel beam needs no scan: its start is the difference of the two values
+ * compared (ParaDisCUDA2d.cu:56-62), which is >= 0 in any rounding. */
+
+static int FN(flat_start_hazard)(int xb, T p0, T pint, T dpc0, T s, T c, T srcx, T srcy,
+                                 double u0, T di, double margin)
+{
+    const double tie = 2e-6 * fmax(fabs((double)p0), fabs((double)dpc0));
+    (void)pint;
+    if (!(p0 >= dpc0 || fabs((double)(p0 - dpc0)) <= tie)) return 0;
+    const T back = xb ? srcy * p0 / ((p0 - srcx) * s / c + srcy)
+                      : srcx * p0 / ((p0 - srcy) * c / s + srcx);
+    const T col0 = xb ? (T)(u0 * (double)c) : (T)(u0 * (double)s);
+    return ((double)((back - col0) / di) < margin);
+}
+
+static int FN(arc_start_hazard)(int xb, T p0, T pint, T dpc0, T srcx, T srcy, T base,
+                                double det_half_minus_c0, int flag, T colsz, double margin)
+{
+    T tan0, tan1;
+    if (xb) {
+        tan0 = ((srcx - p0) == 0) ? (T)1e10 : srcy / (srcx - p0);
+        tan1 = (base == 0) ? (T)1e10 : (T)(-1 / tan((double)base));
+    } else {
+        tan0 = (srcy - p0) / srcx;
+        tan1 = (T)(-1 / tan((double)base));
+    }
+    const T delta = (T)atan((double)((tan0 - tan1) / (1 + tan0 * tan1)));
+    const double v = det_half_minus_c0 + (double)(delta * (T)flag / colsz);
+    if (v >= 10 * margin) return 0;
+    return ((double)((dpc0 - p0) / pint) < margin);
+}
+
+long long FN(ddo_scan2d)(const ddo_geom2 *g, int geom, const float *angles, double margin,
+                         int *per_view)
+{
+    if (per_view)
+        for (int v = 0; v < g->nv; v++) per_view[v] = 0;
+    if (geom == DDO_PARA) return 0;
+    const int W = g->width, H = g->height, D = g->nd;
+    const T sx = (T)g->pix_x, sy = (T)g->pix_y, ds = (T)g->det_size;
+    const T R = (T)g->iso_source, SDD = (T)g->source_detector;
+    const T pxs = (T)g->pix_xshift, pys = (T)g->pix_yshift, bin = (T)g->bin_shift;
+    const T vds = R / SDD * ds, vbs = R / SDD * bin;
+    FN(view2) vw;
+    vw.dp = (T *)malloc(sizeof(T) * (D + 1));
+    vw.bcoef = (T *)malloc(sizeof(T) * (D + 1));
+    long long count = 0;
+    for (int v = 0; v < g->nv; v++) {
+        const T view = (T)angles[v];
+        FN(setup_view2)(g, geom, view, &vw);
+        const int xb = vw.xb, nline = xb ? H : W, npix = xb ? W : H;
+        const T axis0 = xb ? (T)(-W / 2.0 * sx + pxs) : (T)(-H / 2.0 * sy + pys);
+        const T axis1 = xb ? (T)(W / 2.0 * sx + pxs) : (T)(H / 2.0 * sy + pys);
+        for (int line = 0; line < nline; line++) {
+            const T lpos = xb ? (T)((H / 2.0 - line - 0.5) * sy + pys)
+                              : (T)((line - W / 2.0 + 0.5) * sx + pxs);
+            const T p0 = xb ? FN(map2x)(vw.srcx, vw.srcy, axis0, lpos)
+                            : FN(map2y)(vw.srcx, vw.srcy, lpos, axis0);
+            const T p1 = xb ? FN(map2x)(vw.srcx, vw.srcy, axis1, lpos)
+                            : FN(map2y)(vw.srcx, vw.srcy, lpos, axis1);
+            const T pint = (p1 - p0) / (T)npix;
+            for (int c0 = 0; c0 < D; c0 += 256) {
+                int hz;
+                if (geom == DDO_FLAT) {
+                    const double u0 = vw.flip ? (D / 2.0 - c0) * vds + vbs : (c0 - D / 2.0) * vds + vbs;
+                    hz = FN(flat_start_hazard)(xb, p0, pint, vw.dp[c0], vw.s, vw.c, vw.srcx,
+                                               vw.srcy, u0, vw.di, margin);
+                } else {
+                    hz = FN(arc_start_hazard)(xb, p0, pint, vw.dp[c0], vw.srcx, vw.srcy,
+                                              bin + view, D / 2.0 - c0, vw.flag, ds, margin);
+                }
+                count += hz;
+                if (per_view) per_view[v] += hz;
+            }
+        }
+    }
+    free(vw.dp);
+    free(vw.bcoef);
+    return count;
+}
+
+long long FN(ddo_scan3d)(const ddo_geom3 *g, int geom, const float *angles, const float *sp,
+                         double margin, int *per_view)
+{
+    if (geom == DDO_SPIRAL && !sp) return -1;
+    if (per_view)
+        for (int v = 0; v < g->nv; v++) per_view[v] = 0;
+    const int W = g->width, H = g->height, C = g->ncol;
+    const T sx = (T)g->pix_x, sy = (T)g->pix_y;
+    const T pxs = (T)g->pix_xshift, pys = (T)g->pix_yshift;
+    FN(view3) w;
+    w.dp = (T *)malloc(sizeof(T) * (C + 1));
+    w.mag = (T *)malloc(sizeof(T) * (C + 1));
+    long long count = 0;
+    for (int v = 0; v < g->nv; v++) {
+        const T view = (T)angles[v];
+        FN(setup_view3)(g, geom, view, sp, v, &w);
+        const int xb = w.xb, nline = xb ? H : W, npix = xb ? W : H;
+        const T axis0 = xb ? (T)(-W / 2.0 * sx + pxs) : (T)(-H / 2.0 * sy + pys);
+        const T axis1 = xb ? (T)(W / 2.0 * sx + pxs) : (T)(H / 2.0 * sy + pys);
+        for (int line = 0; line < nline; line++) {
+            const T lpos = xb ? (T)((H / 2.0 - line - 0.5) * sy + pys)
+                              : (T)((line - W / 2.0 + 0.5) * sx + pxs);
+            const T p0 = xb ? FN(map2x)(w.srcx, w.srcy, axis0, lpos)
+                            : FN(map2y)(w.srcx, w.srcy, lpos, axis0);
+            const T p1 = xb ? FN(map2x)(w.srcx, w.srcy, axis1, lpos)
+                            : FN(map2y)(w.srcx, w.srcy, lpos, axis1);
+            const T pint = (p1 - p0) / (T)npix;
+            for (int c0 = 0; c0 < C; c0 += 256) {
+                int hz;
+                if (geom == DDO_CONE_FLAT) {
+                    const double u0 = w.flip ? (C / 2.0 - c0) * w.vds + w.vbs
+                                             : (c0 - C / 2.0) * w.vds + w.vbs;
+                    hz = FN(flat_start_hazard)(xb, p0, pint, w.dp[c0], w.s, w.c, w.srcx,
+                                               w.srcy, u0, w.di, margin);
+                } else {
+                    hz = FN(arc_start_hazard)(xb, p0, pint, w.dp[c0], w.srcx, w.srcy,
+                                              w.colshift + w.view, C / 2.0 - c0, w.flag,
+                                              w.colsz, margin);
+                }
+                count += hz;
+                if (per_view) per_view[v] += hz;
+            }
+        }
+    }
+    free(w.dp);
+    free(w.mag);
+    return count;
+}

@@ -60,3 +60,46 @@ def inputs(case, batch=2, seed=0):
     x = rng.random((batch, D, H, W)).astype(np.float32)
     y = rng.random((batch, len(ang), R, C)).astype(np.float32)
     return x, y
+
+
+def ellipsoids(D, H, W, n, seed, scale=1.0):
+    """Sum of n seeded random ellipsoids (intensity U[0, 1] x scale), rasterised
+    at voxel centres in FP64 (the same bits on every host)."""
+    rng = np.random.default_rng(seed)
+    zz, yy, xx = np.mgrid[0:D, 0:H, 0:W].astype(np.float64)
+    vol = np.zeros((D, H, W))
+    for _ in range(n):
+        c = [rng.uniform(0.2, 0.8) * s for s in (D, H, W)]
+        ax = [rng.uniform(0.05, 0.3) * s for s in (D, H, W)]
+        vol[((zz - c[0]) / ax[0]) ** 2 + ((yy - c[1]) / ax[1]) ** 2 + ((xx - c[2]) / ax[2]) ** 2 <= 1] += \
+            rng.uniform(0, 1)
+    return (vol * scale).astype(np.float32)
+
+
+def cone_256cube():
+    """The cone-beam configuration: 256^3 at 1 mm, 512 x 384 detector of
+    1 mm cells, SID 500 / SDD 1000, 360 views over 360 degrees."""
+    opt = np.array([256, 256, 256, 512, 384, 1.0, 1.0, 1.0, 1.0, 1.0, 500.0, 1000.0, 0, 0, 0, 0, 0], np.float32)
+    return opt, (np.arange(360) * 2 * np.pi / 360).astype(np.float32)
+
+
+def spiral_512x128():
+    """The spiral configuration: 512 x 512 x 128 at 0.66 x 0.66 x 1 mm, 64 x 736
+    arc detector (1.2858 mm columns at SDD 1085.6, 1 mm rows), 1152 views per
+    turn, pitch 1, 3 turns, trajectory centred on the volume."""
+    V = 3456
+    p = 1.0 * 64 * 1.0 * 595.0 / 1085.6 / 1152
+    opt = np.array([512, 512, 128, 736, 64, 0.66, 0.66, 1.0, 1.2858 / 1085.6, 1.0, 595.0, 1085.6, 0.0, 0.0,
+                    0.0, 0.0], np.float32)
+    ang = (np.arange(V) * 2 * np.pi / 1152).astype(np.float32)
+    return opt, ang, spiral_source(V, p, -p * (V - 1) / 2)
+
+
+# view subsets of the full configurations kept as golden vectors, with the
+# strides that subsample their outputs (full outputs would be tens of MB)
+CONE_VIEWS = np.array([0, 45, 100, 271])
+SPIRAL_VIEWS = np.array([0, 700, 1500, 1728, 2600, 3455])
+CONE_SINO_STRIDE = (slice(None), slice(None), slice(None, None, 4), slice(None))      # (B, V, R, C)
+CONE_VOL_STRIDE = (slice(None), slice(None, None, 8), slice(None, None, 4), slice(None, None, 4))
+SPIRAL_SINO_STRIDE = (slice(None), slice(None), slice(None, None, 2), slice(None))
+SPIRAL_VOL_STRIDE = (slice(None), slice(None, None, 4), slice(None, None, 8), slice(None, None, 8))

@@ -6,6 +6,11 @@ oracle/_ref/libddref.so by `make -C oracle`):
     python tests/golden/make_golden.py               # operator outputs -> dd2d_golden.npz
     python tests/golden/make_golden.py --sysmatrix   # system matrices  -> sysmat_golden.npz
     python tests/golden/make_golden.py --fbp         # FBP              -> fbp_golden.npz
+    python tests/golden/make_golden.py --cuda3d [--out PATH]   # 3-D -> dd3d_golden.npz
+
+The --cuda3d mode runs deeprecon's own CUDA kernels (the reference for the
+3-D geometries, which have no CPU path) and so needs a GPU and the fatbins
+that `make -C oracle` compiles from the reference sources (oracle/refcuda.py).
 
 Every case stores its seeded inputs and the reference outputs (computed by
 the unmodified deeprecon CPU projectors, single-threaded), so the tests can
@@ -199,8 +204,65 @@ def main_fbp():
     print("wrote", path, os.path.getsize(path) // 1024, "KB")
 
 
+def main_cuda3d(path):
+    """deeprecon's CUDA outputs for the 18 3-D operators on the small cases of
+    tests/cases3d.py (batch 1, inputs from cases3d.inputs(seed=31)), and for
+    Proj / ProjTrans on view subsets of the full cone-beam and spiral
+    configurations (outputs subsampled by the strides in cases3d)."""
+    import torch
+
+    sys.path.insert(0, os.path.dirname(HERE))
+    import cases3d
+    from oracle import refcuda
+    if not refcuda.available():
+        raise SystemExit("reference CUDA fatbins absent: run make -C oracle where the reference sources exist")
+    dev = torch.device("cuda:0")
+
+    def ref(geom, op, x, ang, opt, sp=None):
+        assert oracle.scan_hazards(geom, ang, opt, sp).sum() == 0, (geom, op)
+        xt = torch.from_numpy(np.ascontiguousarray(x, np.float32))[:, None].to(dev)
+        at = torch.from_numpy(np.ascontiguousarray(ang, np.float32)).to(dev)
+        st = None if sp is None else torch.from_numpy(np.ascontiguousarray(sp, np.float32)).to(dev)
+        y = refcuda.run(geom, op, xt, at, opt, st)
+        torch.cuda.synchronize()
+        return y[:, 0].cpu().numpy()
+
+    out = {}
+    for name, case in sorted(cases3d.cases().items()):
+        geom, opt, ang, sp = case
+        x, y = cases3d.inputs(case, batch=1, seed=31)
+        out[f"{name}/options"] = opt
+        out[f"{name}/angles"] = ang
+        if sp is not None:
+            out[f"{name}/source_pos"] = sp
+        for op in cases3d.OPS:
+            out[f"{name}/{op}/ref"] = ref(geom, op, x if op in cases3d.IMAGE_IN else y, ang, opt, sp)
+
+    opt, ang = cases3d.cone_256cube()
+    sel = cases3d.CONE_VIEWS
+    x = cases3d.ellipsoids(256, 256, 256, 12, 4)[None]
+    yv = np.random.default_rng(5).random((1, sel.size, 384, 512)).astype(np.float32)
+    out["cone256/x_sum"] = np.float64(x.sum(dtype=np.float64))
+    out["cone256/proj/ref"] = ref("cone_flat", "proj", x, ang[sel], opt)[cases3d.CONE_SINO_STRIDE]
+    out["cone256/proj_t/ref"] = ref("cone_flat", "proj_t", yv, ang[sel], opt)[cases3d.CONE_VOL_STRIDE]
+
+    opt, ang, sp = cases3d.spiral_512x128()
+    sel = cases3d.SPIRAL_VIEWS
+    x = cases3d.ellipsoids(128, 512, 512, 12, 6, 0.04)[None]
+    yv = np.random.default_rng(7).random((1, sel.size, 64, 736)).astype(np.float32)
+    out["spiral512/x_sum"] = np.float64(x.sum(dtype=np.float64))
+    out["spiral512/proj/ref"] = ref("spiral", "proj", x, ang[sel], opt, sp[:, sel])[cases3d.SPIRAL_SINO_STRIDE]
+    out["spiral512/proj_t/ref"] = ref("spiral", "proj_t", yv, ang[sel], opt, sp[:, sel])[cases3d.SPIRAL_VOL_STRIDE]
+    out["device"] = np.array(torch.cuda.get_device_name(0))
+    np.savez_compressed(path, **out)
+    print("wrote", path, os.path.getsize(path) // 1024, "KB")
+
+
 if __name__ == "__main__":
-    if "--sysmatrix" in sys.argv[1:]:
+    if "--cuda3d" in sys.argv[1:]:
+        args = sys.argv[1:]
+        main_cuda3d(args[args.index("--out") + 1] if "--out" in args else os.path.join(HERE, "dd3d_golden.npz"))
+    elif "--sysmatrix" in sys.argv[1:]:
         main_sysmatrix()
     elif "--fbp" in sys.argv[1:]:
         main_fbp()
