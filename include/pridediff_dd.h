@@ -161,6 +161,25 @@ int dd2d_batch_dc_step(int scan, const dd_instance2d *inst, int n, const void *p
  * synchronous. */
 int dd2d_batch_status(int scan, const dd_instance2d *inst, int n, const void *workspace, int *status);
 
+/* ---- device-side timeouts -------------------------------------------------
+ * No counterpart in the reference (it checks no CUDA error at all,
+ * RadonTorch.cpp:12-14 is its only validation).  Every wait of a kernel on an
+ * asynchronous copy is bounded; a wait that gives up makes the kernel skip
+ * the rest of its work, let its copies in flight land, record DD_ERR_TIMEOUT
+ * and return, so the context stays usable.  The record is kept in the
+ * status word of the call's workspace, read synchronously by: */
+/* dd2d_apply / dd_<Name>Dis2d on `workspace` (same arguments as the call) */
+int dd2d_status(int scan, int op, const dd_geom2d *g, int batch, int num_view, const void *workspace,
+                int *status);
+/* dd2d_apply_planned / dd2d_dc_step on `workspace` (the apply workspace) */
+int dd2d_planned_status(int op, const dd_geom2d *g, int batch, int num_view, const void *workspace,
+                        int *status);
+/* and, without any synchronisation, in one word of pinned, device-mapped
+ * host memory registered here (per device: call once with each device
+ * current; NULL unregisters).  Kernels write DD_ERR_TIMEOUT into it with a
+ * system-scope atomic; the caller reads and clears it. */
+int dd_set_status_sink(int *pinned_host_word);
+
 /* ---- 2-D: named entries, one per radontorch function --------------------
  * Same arguments as dd2d_apply without scan/op.  Each replaces the pybind
  * function of the same name (RadonTorch.cpp:1376-1393). */
@@ -237,6 +256,12 @@ int dd3d_apply_planned(int scan, int op, const dd_geom3d *g, const void *plan, c
 size_t dd3d_dc_workspace_bytes(int scan, const dd_geom3d *g, int batch, int num_view);
 int dd3d_dc_step(int scan, const dd_geom3d *g, const void *plan, float *x, const float *y, float *resid,
                  float eta, int batch, int num_view, void *workspace, size_t workspace_bytes, dd_stream_t stream);
+/* Status word (DD_OK or DD_ERR_TIMEOUT) of the last dd3d_apply on `workspace`
+ * (same arguments as the call), or of the last dd3d_apply_planned on its
+ * apply workspace; synchronous (see "device-side timeouts" above). */
+int dd3d_status(int scan, int op, const dd_geom3d *g, int batch, int num_view, const void *workspace,
+                int *status);
+int dd3d_planned_status(int op, const dd_geom3d *g, int batch, int num_view, const void *workspace, int *status);
 
 /* named entries, one per 3-D radontorch function (RadonTorch.cpp:1395-1414) */
 #define DD_NAMED3D(name)                                                                          \
@@ -275,6 +300,11 @@ DD_NAMED3D(BackProjTransWeightedSpiralDis3d);   /* RadonTorch.cpp:1228 */
  * capture.  Calls share the buffer: calls that overlap on the GPU race. */
 int dd_ProjFanFlatDis2d_noalloc(const dd_geom2d *g, const float *in, float *out, const float *angles,
                                 int batch, int num_view, dd_stream_t stream);
+/* Status word (DD_OK or DD_ERR_TIMEOUT) of the last no-allocation call on the
+ * current device, read from the library's buffer; synchronous.  The buffer's
+ * address is resolved once per device and kept: do not call these after
+ * cudaDeviceReset on that device. */
+int dd_noalloc_status(int *status);
 
 /* ---- diagnostics ----------------------------------------------------------
  * No counterpart in the reference (it has no instrumentation).  Kernel kinds

@@ -9,8 +9,9 @@ CUDA kernels in ``libpridediff_dd.so`` through a plain C ABI
 from . import _native
 from . import radontorch
 from .projector import projector2d, projector3d, projectorsp
+from .status import device_status
 
-__all__ = ["projector2d", "projector3d", "projectorsp", "radontorch", "build"]
+__all__ = ["projector2d", "projector3d", "projectorsp", "radontorch", "build", "device_status"]
 
 
 def build(force: bool = False) -> str:

@@ -39,22 +39,36 @@ def _nvcc() -> str:
     return "nvcc"
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+# Build variants: the product library, and a test-only copy whose bounded
+# waits give up at once (DD_WAIT_LIMIT=0) so that the timeout path -- skip the
+# work, let the copies in flight land, record DD_ERR_TIMEOUT, return -- runs
+# on a GPU without a fault or a hang.  The variant is never loaded by the
+# package itself.
+VARIANTS = {None: [], "waittest": ["-DDD_WAIT_LIMIT=0"]}
+
+
+def lib_path(variant=None) -> str:
+    return LIB_PATH if variant is None else os.path.join(_BUILD, variant, "libpridediff_dd.so")
+
+
+def build(force: bool = False, verbose: bool = False, variant=None) -> str:
     """Compile every translation unit for sm_103a and link the shared library."""
-    os.makedirs(_BUILD, exist_ok=True)
+    out_path = lib_path(variant)
+    bdir = os.path.dirname(out_path)
+    os.makedirs(bdir, exist_ok=True)
     srcs = [os.path.join(_CSRC, s) for s in SOURCES]
-    deps = srcs + [os.path.join(_CSRC, f) for f in os.listdir(_CSRC) if f.endswith(".cuh")] + \
+    deps = srcs + [os.path.join(_CSRC, f) for f in os.listdir(_CSRC) if f.endswith((".cuh", ".h"))] + \
         [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
-    if not force and os.path.exists(LIB_PATH):
-        lib_m = os.path.getmtime(LIB_PATH)
+    if not force and os.path.exists(out_path):
+        lib_m = os.path.getmtime(out_path)
         if all(os.path.getmtime(d) <= lib_m for d in deps):
-            return LIB_PATH
+            return out_path
     nvcc = _nvcc()
-    objs = [os.path.join(_BUILD, os.path.splitext(s)[0] + ".o") for s in SOURCES]
+    objs = [os.path.join(bdir, os.path.splitext(s)[0] + ".o") for s in SOURCES]
 
     def compile_one(pair):
         src, obj = pair
-        cmd = [nvcc, *NVCC_FLAGS, "-c", src, "-o", obj]
+        cmd = [nvcc, *NVCC_FLAGS, *VARIANTS[variant], "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -63,13 +77,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, len(srcs))) as ex:
         list(ex.map(compile_one, zip(srcs, objs)))
-    tmp = LIB_PATH + ".tmp"
+    tmp = out_path + ".tmp"
     r = subprocess.run([nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs, "-lcudart"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, out_path)
+    return out_path
 
 
 class _Geom2d(ctypes.Structure):
@@ -183,6 +197,19 @@ def _declare(lib):
     lib.dd_status_string.argtypes = [i]
     lib.dd_version.restype = cp
     lib.dd_version.argtypes = []
+    ip_ = ctypes.POINTER(ctypes.c_int)
+    lib.dd2d_status.restype = i
+    lib.dd2d_status.argtypes = [i, i, g2, i, i, vp, ip_]
+    lib.dd2d_planned_status.restype = i
+    lib.dd2d_planned_status.argtypes = [i, g2, i, i, vp, ip_]
+    lib.dd3d_status.restype = i
+    lib.dd3d_status.argtypes = [i, i, g3, i, i, vp, ip_]
+    lib.dd3d_planned_status.restype = i
+    lib.dd3d_planned_status.argtypes = [i, g3, i, i, vp, ip_]
+    lib.dd_set_status_sink.restype = i
+    lib.dd_set_status_sink.argtypes = [vp]
+    lib.dd_noalloc_status.restype = i
+    lib.dd_noalloc_status.argtypes = [ip_]
     lib.dd_fbp_filter.restype = i
     lib.dd_fbp_filter.argtypes = [vp, vp, vp, i, vp, ctypes.c_longlong, i, vp]
 
@@ -201,6 +228,14 @@ def load():
             _declare(lib)
             _lib = lib
         return _lib
+
+
+def load_variant(variant: str):
+    """A test-only build variant (see VARIANTS), built on first use."""
+    path = build(variant=variant)
+    lib = ctypes.CDLL(path)
+    _declare(lib)
+    return lib
 
 
 def status_string(code: int) -> str:

@@ -25,6 +25,7 @@ from typing import List, Optional, Sequence
 import torch
 
 from . import _native as N
+from . import status as _status
 from .radontorch import host_options
 
 
@@ -113,6 +114,7 @@ class UnevenBatch2d:
         if x.numel() != (self.img_numel if fwd else self.sino_numel) or not x.is_contiguous():
             raise RuntimeError("packed input has the wrong size or is not contiguous")
         out = torch.empty(self.sino_numel if fwd else self.img_numel, dtype=torch.float32, device=self.device)
+        _status.check(self.device)
         with torch.cuda.device(self.device):
             st = lib.dd2d_batch_apply(self.sc, N.OPS[op], self.inst, self.n, self.plan.data_ptr(), x.data_ptr(),
                                       out.data_ptr(), self.workspace.data_ptr(), self.workspace.numel(),
@@ -137,6 +139,7 @@ class UnevenBatch2d:
         lib = N.load()
         if x.numel() != self.img_numel or y.numel() != self.sino_numel:
             raise RuntimeError("packed x / y have the wrong size")
+        _status.check(self.device)
         with torch.cuda.device(self.device):
             st = lib.dd2d_batch_dc_step(self.sc, self.inst, self.n, self.plan.data_ptr(), x.data_ptr(),
                                         y.data_ptr(), float(eta), self.workspace.data_ptr(),

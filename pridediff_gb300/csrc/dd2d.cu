@@ -170,7 +170,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.sub = sub;
     if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW, kFwdCluster>(g, op, it, smem, g.num_det, rsmax, ph) &&
         threadIdx.x == 0)
-        atomicExch(status, DD_ERR_TIMEOUT);
+        dd_report_timeout(status);
 }
 
 // Parallel beam (plan time): the views that walk image rows and those that
@@ -270,9 +270,13 @@ k_adj_para(dd_geom2d g, int B, int V, int nl, int axis, const int *__restrict__ 
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
         // past this barrier every warp has finished view idx - 1, whose
-        // buffer takes the copies of view idx + 1 (none is in flight on abort)
+        // buffer takes the copies of view idx + 1
         __syncthreads();
-        if (abort_flag) break;
+        if (abort_flag) {
+            // view idx's copies (the wait gave up on them) may be in flight
+            if (tid == issuer) dd_mbar_drain(&bar[buf], ph.parity(buf) ^ 1u);
+            break;
+        }
         if (tid == issuer && idx + 1 < nv) issue(idx + 1, buf ^ 1);
         const DdLine &L = rec[buf], &Ld = drec[buf];
         if (L.h.npiece == 0) continue;   // the same for the whole CTA
@@ -313,7 +317,7 @@ k_adj_para(dd_geom2d g, int B, int V, int nl, int axis, const int *__restrict__ 
     }
     __syncthreads();
     if (abort_flag) {
-        if (tid == 0) atomicExch(status, DD_ERR_TIMEOUT);
+        if (tid == 0) dd_report_timeout(status);
         return;
     }
     for (int b = 0; b < nb; b++) {
@@ -428,7 +432,7 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     bool ok;
     if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(g, it, smem, ph);
     else ok = adj_tile_map<GEOM, OPK>(g, it, smem, ph);
-    if (!ok && threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+    if (!ok && threadIdx.x == 0) dd_report_timeout(status);
 }
 
 // ---------------------------------------------------------------------------
@@ -785,6 +789,44 @@ extern "C" int dd2d_dc_step(int scan, const dd_geom2d *g, const void *planp, flo
     if (s1 != DD_OK) return s1;
     return apply_planned(scan, DD_OP_PROJ_T, g, planp, resid, x, batch, num_view, workspace, workspace_bytes,
                          s, nullptr, x, -eta);
+}
+
+static int read_word(const void *p, int *status) {
+    if (cudaMemcpy(status, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DD_ERR_LAUNCH;
+    return DD_OK;
+}
+
+extern "C" int dd2d_status(int scan, int op, const dd_geom2d *g, int batch, int num_view, const void *workspace,
+                           int *status) {
+    if (validate(scan, op, g, batch, num_view) != DD_OK || !workspace || !status) return DD_ERR_INVALID_ARG;
+    const size_t pb = plan_layout(scan, g, num_view, !op_is_forward(op)).total;
+    return read_word((const char *)workspace + pb + apply_layout(op, g, batch, num_view).status, status);
+}
+
+extern "C" int dd2d_planned_status(int op, const dd_geom2d *g, int batch, int num_view, const void *workspace,
+                                   int *status) {
+    if (!g || batch <= 0 || num_view <= 0 || !workspace || !status) return DD_ERR_INVALID_ARG;
+    return read_word((const char *)workspace + apply_layout(op, g, batch, num_view).status, status);
+}
+
+// byte offset of the status word of a dd2d_apply call in its workspace (used by
+// the no-allocation entry point, whose workspace is the library's own buffer)
+size_t dd2d_status_offset(int scan, int op, const dd_geom2d *g, int batch, int num_view) {
+    return plan_layout(scan, g, num_view, !op_is_forward(op)).total + apply_layout(op, g, batch, num_view).status;
+}
+
+// each translation unit with bounded waits keeps its own sink pointer
+int dd2b_set_sink(int *sink);   // dd2d_batch.cu
+int dd3_set_sink(int *sink);    // dd3d.cu
+
+extern "C" int dd_set_status_sink(int *sink) {
+    int *dev_ptr = nullptr;
+    if (sink && cudaHostGetDevicePointer((void **)&dev_ptr, sink, 0) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return DD_ERR_INVALID_ARG;   // not pinned, device-mapped host memory
+    }
+    if (dd_set_status_sink_tu(dev_ptr) || dd2b_set_sink(dev_ptr) || dd3_set_sink(dev_ptr)) return DD_ERR_LAUNCH;
+    return DD_OK;
 }
 
 // named entries (RadonTorch.cpp:1376-1393)

@@ -244,7 +244,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
         }
         __syncthreads();   // every thread passed the cluster barrier above before s_it changes
         if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdItemsCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
-            if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+            if (threadIdx.x == 0) dd_report_timeout(status);
             break;
         }
     }
@@ -298,7 +298,7 @@ k_adj_items(const BatchInst *__restrict__ desc, const int4 *__restrict__ items, 
         if constexpr (GEOM == DD_GEOM_PARA) ok = adj_tile<GEOM, OPK>(s_g, s_it, smem, ph);
         else ok = adj_tile_map<GEOM, OPK>(s_g, s_it, smem, ph);
         if (!ok) {
-            if (threadIdx.x == 0) atomicExch(status, DD_ERR_TIMEOUT);
+            if (threadIdx.x == 0) dd_report_timeout(status);
             break;
         }
     }
@@ -564,6 +564,8 @@ extern "C" int dd2d_batch_dc_step(int scan, const dd_instance2d *inst, int n, co
     if (s1 != DD_OK) return s1;
     return batch_adjoint(scan, DD_OP_PROJ_T, L, pb, resid, x, x, -eta, wb, tune, st);
 }
+
+int dd2b_set_sink(int *sink) { return dd_set_status_sink_tu(sink); }
 
 extern "C" int dd2d_batch_status(int scan, const dd_instance2d *inst, int n, const void *ws, int *status) {
     if (validate_batch(scan, DD_OP_PROJ, inst, n) != DD_OK || !ws || !status) return DD_ERR_INVALID_ARG;

@@ -389,7 +389,12 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         // past this barrier every warp has finished line - 1, whose buffer
         // takes the copies of line + 1
         __syncthreads();
-        if (abort_flag) break;
+        if (abort_flag) {
+            // this line's copies may still be in flight (the next line's are
+            // issued only after this wait): let them land before returning
+            if (tid == issuer) dd_mbar_drain(&bar[buf], ph.parity(buf) ^ 1u);
+            break;
+        }
         if (tid == issuer && line + CL < nline) issue(line + CL, buf ^ 1);
         const DdLine &R = rec[buf];
         const int np = R.h.npiece;
@@ -493,7 +498,7 @@ __device__ bool fwd_view(const dd_geom2d &g, int op, const FwdItem &it, unsigned
         }
     }
     // no copy is left in flight here: the next line's copies are issued only
-    // after its predecessor's wait succeeded
+    // after its predecessor's wait succeeded, and an abort drained its line's
     __syncthreads();   // the next item's first copies reuse the buffers
     if constexpr (CL > 1) {
         // ranks > 0 leave their sums in the (idle) line-table space; rank 0
@@ -777,6 +782,8 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
         ph.flip(buf);
         __syncthreads();
         if (abort_flag) {
+            // view v's copies (not waited for) and view v + 1's may be in flight
+            if (tid == 0) dd_mbar_drain(&bar[buf], ph.parity(buf) ^ 1u);
             inflight = (v + 1 < V) ? (buf ^ 1) : -1;
             break;
         }
@@ -902,7 +909,7 @@ __device__ bool adj_tile(const dd_geom2d &g, const AdjItem &it, unsigned char *s
         __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
     if (abort_flag) {
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], ph.parity(inflight));
+        if (tid == 0 && inflight >= 0) dd_mbar_drain(&bar[inflight], ph.parity(inflight));
         if (inflight >= 0) ph.flip(inflight);
         __syncthreads();
         return false;
@@ -1042,6 +1049,8 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         // one barrier per view: past it every warp has finished view v - 1
         __syncthreads();
         if (abort_flag) {
+            // view v's copies (not waited for) may still be in flight
+            if (tid == 0) dd_mbar_drain(&bar[buf], ph.parity(buf) ^ 1u);
             vstop = v + 1;
             break;
         }
@@ -1159,7 +1168,7 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         // let the copies of view vstop (issued, not waited for) land
         for (int u = vstop; u < V && u < vstop + 1; u++) {
             const int b = u % kAdjBufs;
-            if (tid == 0) dd_mbar_wait(&bar[b], ph.parity(b));
+            if (tid == 0) dd_mbar_drain(&bar[b], ph.parity(b));
             ph.flip(b);
         }
         __syncthreads();

@@ -432,8 +432,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd3(const Fwd3Args a) {
         // let copies still in flight land before the CTA exits
         if (tid == 0) {
             for (int b = 0; b < 2; b++)
-                if (nissue[b] > nwait[b]) dd_mbar_wait(&bar[b], (uint32_t)nwait[b] & 1u);
-            atomicExch(a.status, DD_ERR_TIMEOUT);
+                if (nissue[b] > nwait[b]) dd_mbar_drain(&bar[b], (uint32_t)nwait[b] & 1u);
+            dd_report_timeout(a.status);
         }
         return;
     }
@@ -619,6 +619,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_adj3(const Adj3Args a) {
         ph.flip(buf);
         __syncthreads();
         if (abort_flag) {
+            // view v's copies (the wait gave up on them) and view v + 1's may be in flight
+            if (tid == 0) dd_mbar_drain(&bar[buf], ph.parity(buf) ^ 1u);
             inflight = (v + 1 < vr.y) ? (buf ^ 1) : -1;
             break;
         }
@@ -688,8 +690,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_adj3(const Adj3Args a) {
         __syncthreads();   // buffer `buf` is refilled by the next iteration's issue
     }
     if (abort_flag) {
-        if (tid == 0 && inflight >= 0) dd_mbar_wait(&bar[inflight], ph.parity(inflight));
-        if (tid == 0) atomicExch(a.status, DD_ERR_TIMEOUT);
+        if (tid == 0 && inflight >= 0) dd_mbar_drain(&bar[inflight], ph.parity(inflight));
+        if (tid == 0) dd_report_timeout(a.status);
         return;
     }
     if (!active) return;
@@ -961,6 +963,28 @@ extern "C" int dd3d_dc_step(int scan, const dd_geom3d *g, const void *planp, flo
     if (s1 != DD_OK) return s1;
     return adjoint(scan, DD_OP_PROJ_T, g, pb, resid, x, x, -eta, batch, num_view, wb + A.ss, status + 1, s);
 }
+
+extern "C" int dd3d_status(int scan, int op, const dd_geom3d *g, int batch, int num_view, const void *workspace,
+                           int *status) {
+    if (validate(scan, op, g, batch, num_view) != DD_OK || !workspace || !status) return DD_ERR_INVALID_ARG;
+    const bool f = op_is_forward(op);
+    const size_t off = dd3d_plan_bytes(scan, g, num_view) + apply_layout(f, !f, g, batch, num_view).status;
+    if (cudaMemcpy(status, (const char *)workspace + off, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    return DD_OK;
+}
+
+extern "C" int dd3d_planned_status(int op, const dd_geom3d *g, int batch, int num_view, const void *workspace,
+                                   int *status) {
+    if (!g || batch <= 0 || num_view <= 0 || !workspace || !status) return DD_ERR_INVALID_ARG;
+    const bool f = op_is_forward(op);
+    const size_t off = apply_layout(f, !f, g, batch, num_view).status;
+    if (cudaMemcpy(status, (const char *)workspace + off, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return DD_ERR_LAUNCH;
+    return DD_OK;
+}
+
+int dd3_set_sink(int *sink) { return dd_set_status_sink_tu(sink); }
 
 // named entries (RadonTorch.cpp:1395-1414)
 #define DD_NAMED3(name, scan, op)                                                                          \

@@ -2,14 +2,42 @@
 //
 // Every wait is bounded: a wait that does not complete within
 // DD_WAIT_LIMIT polls reports failure instead of spinning forever, and the
-// kernel records DD_ERR_TIMEOUT in its status word and returns.
+// kernel records DD_ERR_TIMEOUT (dd_report_timeout), lets the copies it has
+// issued and not yet waited for land (dd_mbar_drain, bounded by
+// DD_DRAIN_LIMIT polls) and returns.  A build with a small DD_WAIT_LIMIT
+// makes every wait give up at once while the drain still lets the copies
+// land: that is how the timeout path is tested without a fault or a hang.
 #pragma once
 
+#include <cuda_runtime.h>
 #include <stdint.h>
+
+#include "../../include/pridediff_dd.h"
 
 #ifndef DD_WAIT_LIMIT
 #define DD_WAIT_LIMIT (1u << 26)
 #endif
+#ifndef DD_DRAIN_LIMIT
+#define DD_DRAIN_LIMIT (1u << 26)
+#endif
+
+// Host-visible copy of the timeout status: a word in host-mapped (pinned)
+// memory that the caller registers with dd_set_status_sink.  Each translation
+// unit holds its own copy of this pointer (file scope) and sets it in
+// dd_set_status_sink_tu; kernels write DD_ERR_TIMEOUT there as well as
+// into their workspace status word, so the host sees a timeout without a
+// synchronisation.
+static __device__ int *dd_status_sink = nullptr;
+
+__device__ __forceinline__ void dd_report_timeout(int *status) {
+    if (status) atomicExch(status, DD_ERR_TIMEOUT);
+    int *sink = dd_status_sink;
+    if (sink) atomicExch_system(sink, DD_ERR_TIMEOUT);
+}
+
+static inline int dd_set_status_sink_tu(int *sink) {
+    return cudaMemcpyToSymbol(dd_status_sink, &sink, sizeof(sink)) == cudaSuccess ? 0 : 1;
+}
 
 __device__ __forceinline__ uint32_t dd_smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -62,6 +90,17 @@ struct DdPhases {
 // Bounded wait for the phase with the given parity.  Returns false on timeout.
 __device__ __forceinline__ bool dd_mbar_wait(uint64_t *bar, uint32_t parity) {
     for (uint32_t it = 0; it < DD_WAIT_LIMIT; ++it) {
+        if (dd_mbar_try_wait(bar, parity)) return true;
+        if (it > 64) __nanosleep(32);
+    }
+    return false;
+}
+
+// After a timeout: wait (bounded by DD_DRAIN_LIMIT) for the phase of copies
+// that were issued and not waited for, so that no bulk copy still writes into
+// the CTA's shared memory when it returns.
+__device__ __forceinline__ bool dd_mbar_drain(uint64_t *bar, uint32_t parity) {
+    for (uint32_t it = 0; it < DD_DRAIN_LIMIT; ++it) {
         if (dd_mbar_try_wait(bar, parity)) return true;
         if (it > 64) __nanosleep(32);
     }

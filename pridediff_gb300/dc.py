@@ -19,6 +19,7 @@ import ctypes
 import torch
 
 from . import _native as N
+from . import status as _status
 from .radontorch import _stream_ptr, host_options, plan2d
 
 
@@ -40,6 +41,7 @@ def residual(proj, x: torch.Tensor, y: torch.Tensor, angles: torch.Tensor) -> to
     nbytes = int(lib.dd2d_dc_workspace_bytes(N.SCAN2D[proj.scan_type], g, B, V))
     ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
     # dd2d_dc_step with eta = 0 leaves x unchanged and writes A x - y into `out`
+    _status.check(x.device)
     with torch.cuda.device(x.device):
         st = lib.dd2d_dc_step(N.SCAN2D[proj.scan_type], g, plan.data_ptr(), x.data_ptr(), y.data_ptr(),
                               out.data_ptr(), 0.0, B, V, ws.data_ptr(), nbytes, _stream_ptr(x.device))
@@ -85,6 +87,7 @@ def dc_step(proj, x: torch.Tensor, y: torch.Tensor, angles: torch.Tensor, eta: f
     nbytes = int(lib.dd2d_dc_workspace_bytes(sc, g, B, V))
     if workspace is None or workspace.numel() < nbytes:
         workspace = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
+    _status.check(x.device)
     with torch.cuda.device(x.device):
         st = lib.dd2d_dc_step(sc, g, plan.data_ptr(), x.data_ptr(), y.data_ptr(), resid.data_ptr(), float(eta),
                               B, V, workspace.data_ptr(), workspace.numel(), _stream_ptr(x.device))

@@ -16,13 +16,16 @@ Deliberate differences (all in the caller's favour):
 * ``options`` is read on the host once per (tensor, version) and cached, so
   repeated calls do not synchronise with the device (the reference calls
   ``.item()`` 11-17 times per call, RadonTorch.cpp:19-29);
-* launch and argument errors are reported (the reference checks none).
+* launch and argument errors are reported (the reference checks none), and
+  a device-side wait that timed out in an earlier call makes the next call
+  raise (``status.check``; the reference has no device-side waits).
 """
 from __future__ import annotations
 
 import torch
 
 from . import _native as N
+from . import status as _status
 
 # ---------------------------------------------------------------------------
 # options on the host
@@ -141,6 +144,7 @@ def _apply2d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor)
     if B * C == 0:
         return out.zero_()
     sc, opc = N.SCAN2D[scan], N.OPS[op]
+    _status.check(x.device)
     with torch.cuda.device(x.device):
         # the library validates the geometry before anything is enqueued
         N.check(lib.dd2d_validate(sc, opc, g, B * C, V), f"{scan} {op}")
@@ -199,6 +203,7 @@ def _apply3d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor,
     if B * Ch == 0:
         return out.zero_()
     sc, opc = N.SCAN3D[scan], N.OPS[op]
+    _status.check(x.device)
     with torch.cuda.device(x.device):
         N.check(lib.dd3d_validate(sc, opc, g, B * Ch, V), f"{scan} {op}")
         plan = plan3d(scan, g, angles, source_pos)
@@ -279,6 +284,7 @@ def _sysmatrix(scan: str, options, angles: torch.Tensor) -> torch.Tensor:
     ang = angles.detach().to(dev, torch.float32).contiguous()
     V = int(ang.shape[0])
     sc = N.SCAN2D[scan]
+    _status.check(dev)
     with torch.cuda.device(dev):
         N.check(lib.dd2d_validate(sc, N.OPS["proj"], g, 1, V), f"{scan} system matrix")
         plan = plan2d(scan, g, ang)
