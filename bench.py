@@ -12,6 +12,17 @@ adjoint A^T r for every slice, through projector2d and its autograd pair.
 Metric: FP+BP per second (slice forward + adjoint pairs per second).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
+  python bench.py --micro SCAN --op OP [--batch B] [--views V] [--iters I] [--impl ours|reference]
+
+--micro repeats one operator on a bounded problem and prints its mean
+CUDA-event time (the commands of the profiles/ summaries): SCAN is para, flat
+or arc (the 512^2 fan geometry above), cone_flat or cone_arc (256^3, 512 x 384
+detector, SID 500 / SDD 1000, --views of 360 angles over 360 deg), spiral
+(512 x 512 x 128, 64 x 736 arc detector, the first --views views of the
+comparator's middle turn) or uneven (the 24-instance uneven batch, one persistent launch
+per call; --op proj or proj_t).  With --impl reference it times deeprecon's
+own CUDA kernel for the same operator (built from the reference sources into
+oracle/_ref/cuda where they exist).
 
 On one GPU the line also carries `extra`: the same slices through the plain
 per-slice path (the unbatched comparator), the parallel-beam configuration
@@ -22,9 +33,10 @@ data-consistency loop captured in a CUDA graph, and the 3-D cone-flat and
 spiral configurations, each with its view-swept bytes against the measured
 HBM peak.
 
---impl reference times deeprecon's CPU algorithm on this host (the oracle
-port of it; the reference sources are not present here) on the same
-workload, a bounded sample of slices per step.
+--impl reference times deeprecon's CPU algorithm on this host on the same
+workload, a bounded sample of slices per step: its own build where the
+reference sources were compiled for this host (oracle/_ref), else the FP32
+oracle port, which is bit-identical to it.
 """
 from __future__ import annotations
 
@@ -140,26 +152,52 @@ def ncu_traffic():
         return {}
 
 
-def cpu_port_baseline(seconds=10.0):
-    """deeprecon's CPU algorithm (FP32 oracle port, reference thread rule) on one slice at a time."""
+def _cpu_impl():
+    """deeprecon's CPU fan-flat forward and adjoint on this host: its own build
+    (oracle/_ref/libddref.so, compiled from the reference sources where they
+    exist; an x86 build does not run on another host CPU) or else the FP32
+    oracle port, which is bit-identical to it.  Both split the views over
+    min(ceil(V / 128), cores) threads, the reference's own rule
+    (FanFlatDisCPU2d.cpp:811-813)."""
     import oracle
     oracle.build()
+    threads = oracle.default_threads(GEOM["views"])
+    kind = "port"
+    fwd = lambda x, a: oracle.run2d("flat", "proj", x, a, OPTIONS, "f", threads)     # noqa: E731
+    adj = lambda r, a: oracle.run2d("flat", "proj_t", r, a, OPTIONS, "f", threads)   # noqa: E731
+    if oracle.have_ref():
+        try:
+            z = np.zeros((1, 8, 8), np.float32)
+            oracle.ref2d("flat", "proj", z, np.zeros(2, np.float32), [8, 8, 8, 1, 1, 1, 500, 1000, 0, 0, 0])
+            kind = "reference"
+            fwd = lambda x, a: oracle.ref2d("flat", "proj", x, a, OPTIONS)      # noqa: E731
+            adj = lambda r, a: oracle.ref2d("flat", "proj_t", r, a, OPTIONS)    # noqa: E731
+        except OSError:
+            pass
+    return kind, threads, fwd, adj
+
+
+def cpu_port_baseline(seconds=10.0):
+    """deeprecon's CPU algorithm on one slice at a time (see _cpu_impl)."""
+    kind, threads, fwd, adj = _cpu_impl()
     rng = np.random.default_rng(99)
     ang = angles_np()
     img = phantom(512, 512, 10, rng, 0.04)[None]
     r = rng.standard_normal((1, GEOM["views"], GEOM["num_det"])).astype(np.float32)
-    threads = oracle.default_threads(GEOM["views"])
     n = 0
     t0 = time.perf_counter()
     while True:
-        oracle.run2d("flat", "proj", img, ang, OPTIONS, "f", threads)
-        oracle.run2d("flat", "proj_t", r, ang, OPTIONS, "f", threads)
+        fwd(img, ang)
+        adj(r, ang)
         n += 1
         if time.perf_counter() - t0 >= seconds:
             break
     dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} slice(s) of the workload, forward + exact adjoint, {dt:.1f} s"}
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "host_cpus": os.cpu_count(), "kind": kind,
+            "sample": f"{n} slice(s) of the 16-slice workload, one at a time, forward + exact adjoint, "
+                      f"{dt:.1f} s; FP+BP/s per slice, the unit of the GPU line"
+                      + ("" if kind == "reference" else "; the port takes 1.27x the time of the reference's "
+                         "own build on an x86 host (1.35 vs 1.07 s per slice, identical outputs)")}
 
 
 def run_reference(args):
@@ -167,19 +205,17 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import oracle
-    oracle.build()
+    kind, threads, fwd, adj = _cpu_impl()
     rng = np.random.default_rng(99)
     ang = angles_np()
-    threads = oracle.default_threads(GEOM["views"])
     per_step = 1   # slices per step (bounded sample: one slice of the 16-slice batch)
     imgs = [phantom(512, 512, 10, rng, 0.04)[None] for _ in range(per_step)]
     r = rng.standard_normal((1, GEOM["views"], GEOM["num_det"])).astype(np.float32)
 
     def step():
         for im in imgs:
-            oracle.run2d("flat", "proj", im, ang, OPTIONS, "f", threads)
-            oracle.run2d("flat", "proj_t", r, ang, OPTIONS, "f", threads)
+            fwd(im, ang)
+            adj(r, ang)
 
     for _ in range(args.warmup):
         step()
@@ -192,10 +228,38 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": workload_config(),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{per_step} slice per step (forward + exact adjoint), CPU"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "host_cpus": os.cpu_count(),
+                             "kind": kind,
+                             "sample": f"{per_step} slice of the 16-slice workload per step (forward + exact "
+                                       "adjoint); FP+BP/s per slice, the unit of the GPU line"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    try:
+        line["extra"] = {"reference_cuda": reference_cuda_extra()}
+    except Exception as e:   # report, never hide the reference line
+        line["extra"] = {"reference_cuda": {"error": repr(e)}}
     print(json.dumps(line))
+
+
+def reference_cuda_extra():
+    """deeprecon's own CUDA operators on this host's GPU (the plain-GPU
+    comparator): the workloads of run_comparator_workloads, each step through
+    its CUDA kernels compiled unmodified from the reference sources
+    (oracle/_ref/cuda; absent where those sources were not available)."""
+    import torch
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device on this host"}
+    from oracle import refcuda
+    if not refcuda.available():
+        return {"unavailable": "reference CUDA fatbins absent (built only where the reference sources exist)"}
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)   # noqa: E731
+    res = run_comparator_workloads(dev, flush, ev, refcuda.run)
+    res["what"] = ("deeprecon's CUDA Proj + ProjTrans per loss + backward step, called as radontorch calls "
+                   "them (options read by .item(), per-call texture staging); views where its walk start "
+                   "ties index -1 within rounding are left out (4 cone-beam, 12 spiral)")
+    return res
 
 
 def _ellipsoids(shape, n, seed, scale, dev):
@@ -314,16 +378,7 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
     try:
         from pridediff_gb300.batch import UnevenBatch2d
         from pridediff_gb300 import autotune
-        rng = np.random.default_rng(2024)
-        projs, angs, imgs, nbytes = [], [], [], 0.0
-        for _ in range(24):
-            n = int(rng.choice([256, 384, 512]))
-            V = int(rng.choice([360, 576, 720]))
-            D = int(rng.choice([368, 512, 736]))
-            projs.append(P.projector2d(n, D, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").to(dev))
-            angs.append(torch.arange(V, dtype=torch.float32, device=dev) * (2 * np.pi / V))
-            imgs.append(torch.from_numpy(phantom(n, n, 10, rng, 0.04))[None, None].to(dev))
-            nbytes += 2 * 4.0 * V * (n * n + D)
+        projs, angs, imgs, nbytes = uneven_instances(dev)
         ub = UnevenBatch2d(projs, angs)
         xt = ub.pack(imgs)
         yb = ub.forward(xt)
@@ -347,6 +402,14 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
         del ub, graph, xg, xe, xs, yb, xt
     except Exception as e:
         out["batched_dc_24_uneven"] = {"error": repr(e)}
+    torch.cuda.empty_cache()
+
+    # the workloads of the plain-GPU comparator (deeprecon's own CUDA kernels,
+    # timed by --impl reference), here through this library
+    try:
+        out["same_workloads_as_reference_cuda"] = run_comparator_workloads(dev, flush, ev, None)
+    except Exception as e:
+        out["same_workloads_as_reference_cuda"] = {"error": repr(e)}
     torch.cuda.empty_cache()
 
     # 3-D cone-flat: 2 x 256^3, 360 views, 512 x 384 detector, autograd FP + BP
@@ -424,6 +487,200 @@ def run_extras(dev, flush, peak, step2d, x0, y, B):
     return out
 
 
+def _micro_problem(args, dev):
+    """(geometry, options, input, angles, source_pos) of a --micro run."""
+    import torch
+    import cases3d
+    g = torch.Generator(device=dev).manual_seed(0)
+    image_in = args.op in ("proj", "bproj_t", "bproj_tw")
+    if args.micro in ("para", "flat", "arc"):
+        det = 1.2858 / 1085.6 if args.micro == "arc" else 1.2858
+        opt = [512, 512, 736, 0.66, 0.66, det, 595.0, 1085.6, 0.0, 0.0, 0.0]
+        ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (2 * np.pi / args.views)
+        shape = (args.batch, 1, 512, 512) if image_in else (args.batch, 1, args.views, 736)
+        return opt, torch.rand(shape, device=dev, generator=g), ang, None
+    if args.micro in ("cone_flat", "cone_arc"):
+        col = 1.0 / 1000.0 if args.micro == "cone_arc" else 1.0
+        opt = [256, 256, 256, 512, 384, 1.0, 1.0, 1.0, col, 1.0, 500.0, 1000.0, 0, 0, 0, 0, 0]
+        ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (2 * np.pi / args.views)
+        shape = (args.batch, 1, 256, 256, 256) if image_in else (args.batch, 1, args.views, 384, 512)
+        return opt, torch.rand(shape, device=dev, generator=g), ang, None
+    opt, ang_np, sp_np = cases3d.spiral_512x128()
+    sel = comparator_views()[1][:args.views]   # views of the middle turn
+    ang = torch.from_numpy(ang_np[sel].copy()).to(dev)
+    sp = torch.from_numpy(sp_np[:, sel].copy()).to(dev)
+    shape = (args.batch, 1, 128, 512, 512) if image_in else (args.batch, 1, args.views, 64, 736)
+    return list(opt), torch.rand(shape, device=dev, generator=g) * 0.04, ang, sp
+
+
+def run_micro(args):
+    """--micro: `iters` applications of one operator, mean CUDA-event ms."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    dev = torch.device("cuda:0")
+    if args.micro == "uneven":
+        return run_micro_uneven(args, dev)
+    geo = {"para": "Para", "flat": "FanFlat", "arc": "FanArc", "cone_flat": "ConeFlat", "cone_arc": "ConeArc",
+           "spiral": "Spiral"}[args.micro]
+    dim = "2d" if args.micro in ("para", "flat", "arc") else "3d"
+    name = {"proj": "Proj", "proj_t": "ProjTrans", "bproj": "BackProj", "bproj_t": "BackProjTrans",
+            "bproj_w": "BackProjWeighted", "bproj_tw": "BackProjTransWeighted"}[args.op] + f"{geo}Dis{dim}"
+    opt, x, ang, sp = _micro_problem(args, dev)
+    if args.impl == "reference":
+        import oracle
+        from oracle import refcuda
+        bad = oracle.scan_hazards(args.micro, ang.cpu().numpy(), opt,
+                                  None if sp is None else sp.cpu().numpy()).sum()
+        if bad:
+            raise SystemExit(f"reference kernels not run: {bad} walk starts within rounding of index -1")
+        ot = torch.tensor(opt, dtype=torch.float32)
+        fn = lambda: refcuda.run(args.micro, args.op, x, ang, ot, sp)   # noqa: E731
+        name = "deeprecon CUDA " + name
+    else:
+        from pridediff_gb300 import radontorch
+        f = getattr(radontorch, name)
+        ot = torch.tensor(opt, dtype=torch.float32)
+        fn = (lambda: f(x, ot, ang, sp)) if sp is not None else (lambda: f(x, ot, ang))
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.iters):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    print(f"{name} batch {args.batch}, {int(ang.numel())} views: {a.elapsed_time(b) / args.iters:.3f} ms per call")
+
+
+def uneven_instances(dev, seed=2024, n=24):
+    """The uneven batched configuration: n fan-flat instances with image size,
+    view count and detector count drawn from {256,384,512}^2 x {360,576,720} x
+    {368,512,736}, each with a seeded ellipse phantom."""
+    import torch
+    import pridediff_gb300 as P
+    rng = np.random.default_rng(seed)
+    projs, angs, imgs, nbytes = [], [], [], 0.0
+    for _ in range(n):
+        size = int(rng.choice([256, 384, 512]))
+        V = int(rng.choice([360, 576, 720]))
+        D = int(rng.choice([368, 512, 736]))
+        projs.append(P.projector2d(size, D, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").to(dev))
+        angs.append(torch.arange(V, dtype=torch.float32, device=dev) * (2 * np.pi / V))
+        imgs.append(torch.from_numpy(phantom(size, size, 10, rng, 0.04))[None, None].to(dev))
+        nbytes += 2 * 4.0 * V * (size * size + D)
+    return projs, angs, imgs, nbytes
+
+
+def run_micro_uneven(args, dev):
+    import torch
+    from pridediff_gb300.batch import UnevenBatch2d
+    projs, angs, imgs, _ = uneven_instances(dev)
+    ub = UnevenBatch2d(projs, angs)
+    x = ub.pack(imgs)
+    if args.op == "proj_t":
+        x = ub.forward(x)
+    fn = (lambda: ub.forward(x)) if args.op == "proj" else (lambda: ub.adjoint(x))
+    fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.iters):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    print(f"uneven batch of 24 {args.op}: {a.elapsed_time(b) / args.iters:.3f} ms per call")
+
+
+# Views of the 3-D configurations that deeprecon's CUDA kernels are not run
+# on: on these an image edge ties the first column boundary of a 256-column
+# block to within rounding, where the reference's walk could start at index
+# -1 and read or write out of bounds (tests/test_oracle.py checks these lists
+# against the oracle's start-index scan).  Both sides of the comparator skip
+# them.
+CONE_REF_SKIP = [12, 102, 168, 258]
+SPIRAL_TURN = (1152, 2304)   # the middle of the three turns
+SPIRAL_REF_SKIP = [1267, 1333, 1339, 1555, 1613, 1829, 1835, 1901, 2117, 2123, 2197, 2203]
+
+
+def comparator_views():
+    """(cone-beam view indices, spiral view indices) of the comparator."""
+    cone = np.setdiff1d(np.arange(360), CONE_REF_SKIP)
+    spiral = np.setdiff1d(np.arange(*SPIRAL_TURN), SPIRAL_REF_SKIP)
+    return cone, spiral
+
+
+def run_comparator_workloads(dev, flush, ev, ref):
+    """One loss + backward step (forward A x, residual, exact adjoint) on the
+    headline fan-flat slices, on 2 x 256^3 cone-beam volumes (356 views) and
+    on 2 x 512x512x128 spiral volumes (the middle turn's 1140 views).
+
+    ref=None runs this library's projector modules (autograd).  Otherwise
+    `ref` is deeprecon's CUDA operator (oracle/refcuda.run), called the way
+    radontorch calls it (RadonTorch.cpp:17-83): eleven .item() reads of the
+    device options (RadonTorch.cpp:19-29), an output from torch::empty or
+    torch::zeros, and for the image-reading operators a cudaArray and texture
+    built and freed around the launch (FanFlatDisCUDA2d.cu:777-815)."""
+    import torch
+    import pridediff_gb300 as P
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import cases3d
+    res = {}
+    B = GEOM["batch"]
+    rng = np.random.default_rng(1234)
+    x2 = torch.from_numpy(np.stack([phantom(512, 512, 10, rng, 0.04) for _ in range(B)])[:, None]).to(dev)
+    y2 = torch.from_numpy(rng.random((B, 1, GEOM["views"], GEOM["num_det"]), dtype=np.float32) * 8.0).to(dev)
+    ang2 = torch.from_numpy(angles_np()).to(dev)
+    cone_v, spiral_v = comparator_views()
+    o4, a4 = cases3d.cone_256cube()
+    ang4 = torch.from_numpy(a4[cone_v].copy()).to(dev)
+    x4 = torch.stack([_ellipsoids((256, 256, 256), 12, 40 + i, 1.0, dev) for i in range(2)])[:, None]
+    y4 = torch.rand((2, 1, cone_v.size, 384, 512), device=dev) * 100.0
+    o5, a5, s5 = cases3d.spiral_512x128()
+    ang5 = torch.from_numpy(a5[spiral_v].copy()).to(dev)
+    sp5 = torch.from_numpy(s5[:, spiral_v].copy()).to(dev)
+    x5 = torch.stack([_ellipsoids((128, 512, 512), 12, 60 + i, 0.04, dev) for i in range(2)])[:, None]
+    y5 = torch.rand((2, 1, spiral_v.size, 64, 736), device=dev) * 8.0
+
+    if ref is None:
+        p2 = P.projector2d(512, 736, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").to(dev)
+        p4 = P.projector3d((256, 256, 256), (512, 384), 1.0, 1.0, 500.0, 1000.0, scan_type="flat").to(dev)
+        p5 = P.projectorsp((512, 512, 128), (736, 64), (0.66, 0.66, 1.0), (1.2858, 1.0), 595.0, 1085.6).to(dev)
+
+        def step(proj, x, yy, ang, sp=None):
+            xr = x.detach().requires_grad_(True)
+            fp = proj.projection(xr, ang, sp) if sp is not None else proj.projection(xr, ang)
+            ((fp - yy) ** 2).sum().backward()
+        s2 = lambda: step(p2, x2, y2, ang2)                               # noqa: E731
+        s2_slice = lambda: [step(p2, x2[i:i + 1], y2[i:i + 1], ang2) for i in range(B)]   # noqa: E731
+        s4 = lambda: step(p4, x4, y4, ang4)                               # noqa: E731
+        s5 = lambda: step(p5, x5, y5, ang5, sp5)                          # noqa: E731
+    else:
+        opt2 = torch.tensor(OPTIONS, dtype=torch.float32, device=dev)
+        opt4 = torch.tensor(o4, device=dev)
+        opt5 = torch.tensor(o5, device=dev)
+
+        def step(geom, opt, x, yy, ang, sp=None):
+            fp = ref(geom, "proj", x, ang, [o.item() for o in opt], sp)
+            ref(geom, "proj_t", 2.0 * (fp - yy), ang, [o.item() for o in opt], sp)
+        s2 = lambda: step("flat", opt2, x2, y2, ang2)                     # noqa: E731
+        s2_slice = lambda: [step("flat", opt2, x2[i:i + 1], y2[i:i + 1], ang2) for i in range(B)]   # noqa: E731
+        s4 = lambda: step("cone_flat", opt4, x4, y4, ang4)                # noqa: E731
+        s5 = lambda: step("spiral", opt5, x5, y5, ang5, sp5)              # noqa: E731
+
+    ms = _timed(s2, 3, flush, ev)
+    ms_slice = _timed(s2_slice, 3, flush, ev)
+    res["fan_flat_16x512_720v"] = {"ms_per_step_16_slices_per_call": ms, "value_16_slices_per_call": B / (ms / 1e3),
+                                   "ms_per_step_one_slice_per_call": ms_slice,
+                                   "value_one_slice_per_call": B / (ms_slice / 1e3), "unit": UNIT}
+    ms = _timed(s4, 2, flush, ev)
+    res["cone_flat_2x256^3_356v"] = {"ms_per_step": ms, "value": 2 / (ms / 1e3), "unit": UNIT,
+                                     "views": int(cone_v.size)}
+    ms = _timed(s5, 1, flush, ev)
+    res["spiral_2x512x512x128_1140v"] = {"ms_per_step": ms, "value": 2 / (ms / 1e3), "unit": UNIT,
+                                         "views": int(spiral_v.size)}
+    return res
+
+
 def workload_config():
     return {"workload": "fan-flat DD FP + exact-adjoint BP with autograd, 16 x 512^2 slices, "
                         "720 views over 360 deg, 736 dets x 1.2858 mm, SID 595, SDD 1085.6",
@@ -441,7 +698,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the other configurations (batched DC loop, plain per-slice calls, 3-D)")
+    ap.add_argument("--micro", default=None,
+                    choices=["para", "flat", "arc", "cone_flat", "cone_arc", "spiral", "uneven"],
+                    help="time one operator on a bounded problem instead (see the module docstring)")
+    ap.add_argument("--op", default="proj", choices=["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"])
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--views", type=int, default=720)
+    ap.add_argument("--iters", type=int, default=3)
     args = ap.parse_args()
+    if args.micro:
+        run_micro(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -153,3 +153,16 @@ def test_scan_counts_a_start_that_rounds_below_zero(oracle_mod):
     opt = [W, 41, D, sx, 1.0, ds, R, SDD, 0.0, 0.0, 0.0]
     per = oracle_mod.scan_hazards("flat", np.zeros(1, np.float32), opt)
     assert per[0] >= 1
+
+
+def test_bench_comparator_views_are_the_scan_safe_views(oracle_mod):
+    """bench.py's plain-GPU comparator runs deeprecon's kernels on fixed view
+    lists; they must be exactly the views the scan finds safe."""
+    import bench
+    cone, spiral = bench.comparator_views()
+    opt, ang = cases3d.cone_256cube()
+    assert np.array_equal(cone, oracle_mod.safe_views("cone_flat", ang, opt))
+    opt, ang, sp = cases3d.spiral_512x128()
+    safe = oracle_mod.safe_views("spiral", ang, opt, sp)
+    assert np.array_equal(spiral, safe[(safe >= bench.SPIRAL_TURN[0]) & (safe < bench.SPIRAL_TURN[1])])
+    assert oracle_mod.scan_hazards("flat", bench.angles_np(), bench.OPTIONS).sum() == 0
