@@ -398,7 +398,7 @@ k_trange(dd_geom2d g, int V, const DdView2 *__restrict__ views, const float *__r
     trange[i] = make_int2(kb, kn | (views[v].xb ? 1 << 16 : 0));   // the view's axis in bit 16
 }
 
-// Single-geometry adjoint launch: grid (tiles x, tiles y, image groups).
+// Single-geometry adjoint launch: grid (tiles x * image groups, tiles y).
 template <int GEOM, int OPK>
 __global__ void __launch_bounds__(kThreads)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
@@ -412,9 +412,13 @@ k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
     init_bars(reinterpret_cast<uint64_t *>(smem + SL.bar), GEOM == DD_GEOM_PARA ? 2 : kAdjBufs);
     DdPhases ph;
     AdjItem it;
-    it.c0 = blockIdx.x * kTile;
+    // the image groups of a tile are adjacent in launch order: they run at the
+    // same time, walk the views in step and read each view's map block of the
+    // tile once from DRAM between them (the others hit L2)
+    const int ngroups = (B + kBI - 1) / kBI;
+    it.c0 = (blockIdx.x / ngroups) * kTile;
     it.r0 = blockIdx.y * kTile;
-    it.b0 = blockIdx.z * kBI;
+    it.b0 = (blockIdx.x % ngroups) * kBI;
     it.nb = min(kBI, B - it.b0);
     it.V = V;
     it.nl = nl;
@@ -601,7 +605,8 @@ template <int GEOM>
 static int launch_adj(int op, const dd_geom2d *g, const PlanLayout &P, const char *planb,
                       const float *angles, int B, int V, const float2 *dtab, float *out,
                       const float *base, float scale, int *status, cudaStream_t st) {
-    dim3 grid((g->width + kTile - 1) / kTile, (g->height + kTile - 1) / kTile, (B + kBI - 1) / kBI);
+    const unsigned ngroups = (unsigned)((B + kBI - 1) / kBI);
+    dim3 grid((unsigned)((g->width + kTile - 1) / kTile) * ngroups, (g->height + kTile - 1) / kTile);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
