@@ -12,11 +12,13 @@ adjoint A^T r for every slice, through projector2d and its autograd pair.
 Metric: FP+BP per second (slice forward + adjoint pairs per second).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-extras]
-  python bench.py --micro SCAN --op OP [--batch B] [--views V] [--iters I] [--impl ours|reference]
+  python bench.py --micro SCAN --op OP [--batch B] [--views V] [--size N] [--dets D] [--iters I]
+                  [--impl ours|reference]
 
 --micro repeats one operator on a bounded problem and prints its mean
-CUDA-event time (the commands of the profiles/ summaries): SCAN is para, flat
-or arc (the 512^2 fan geometry above), cone_flat or cone_arc (256^3, 512 x 384
+CUDA-event time (the commands of the profiles/ summaries): SCAN is flat or
+arc (the 512^2 fan geometry above; --size, --dets change it), para (1 mm
+pixels and cells, views over 180 deg), --op fbp for filtered_backprojection, cone_flat or cone_arc (256^3, 512 x 384
 detector, SID 500 / SDD 1000, --views of 360 angles over 360 deg), spiral
 (512 x 512 x 128, 64 x 736 arc detector, the first --views views of the
 comparator's middle turn) or uneven (the 24-instance uneven batch, one persistent launch
@@ -494,10 +496,15 @@ def _micro_problem(args, dev):
     g = torch.Generator(device=dev).manual_seed(0)
     image_in = args.op in ("proj", "bproj_t", "bproj_tw")
     if args.micro in ("para", "flat", "arc"):
-        det = 1.2858 / 1085.6 if args.micro == "arc" else 1.2858
-        opt = [512, 512, 736, 0.66, 0.66, det, 595.0, 1085.6, 0.0, 0.0, 0.0]
-        ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (2 * np.pi / args.views)
-        shape = (args.batch, 1, 512, 512) if image_in else (args.batch, 1, args.views, 736)
+        n, D = args.size or 512, args.dets or 736
+        if args.micro == "para":   # the parallel-beam configuration: 1 mm pixels and cells, 180 deg
+            opt = [n, n, D, 1.0, 1.0, 1.0, 500.0, 1000.0, 0.0, 0.0, 0.0]
+            ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (np.pi / args.views)
+        else:
+            det = 1.2858 / 1085.6 if args.micro == "arc" else 1.2858
+            opt = [n, n, D, 0.66, 0.66, det, 595.0, 1085.6, 0.0, 0.0, 0.0]
+            ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (2 * np.pi / args.views)
+        shape = (args.batch, 1, n, n) if image_in else (args.batch, 1, args.views, D)
         return opt, torch.rand(shape, device=dev, generator=g), ang, None
     if args.micro in ("cone_flat", "cone_arc"):
         col = 1.0 / 1000.0 if args.micro == "cone_arc" else 1.0
@@ -520,6 +527,8 @@ def run_micro(args):
     dev = torch.device("cuda:0")
     if args.micro == "uneven":
         return run_micro_uneven(args, dev)
+    if args.op == "fbp":
+        return run_micro_fbp(args, dev)
     geo = {"para": "Para", "flat": "FanFlat", "arc": "FanArc", "cone_flat": "ConeFlat", "cone_arc": "ConeArc",
            "spiral": "Spiral"}[args.micro]
     dim = "2d" if args.micro in ("para", "flat", "arc") else "3d"
@@ -550,6 +559,31 @@ def run_micro(args):
     b.record()
     torch.cuda.synchronize()
     print(f"{name} batch {args.batch}, {int(ang.numel())} views: {a.elapsed_time(b) / args.iters:.3f} ms per call")
+
+
+def run_micro_fbp(args, dev):
+    """--micro flat|arc|para --op fbp: projector2d.filtered_backprojection
+    (fused weight + filter kernel, then the weighted DD back-projection)."""
+    import torch
+    import pridediff_gb300 as P
+    n, D = args.size or 512, args.dets or 736
+    pix, det = (1.0, 1.0) if args.micro == "para" else (0.66, 1.2858)
+    proj = P.projector2d(n, D, pix, det, 595.0, 1085.6, scan_type=args.micro).to(dev)
+    span = np.pi if args.micro == "para" else 2 * np.pi
+    ang = torch.arange(args.views, dtype=torch.float32, device=dev) * (span / args.views)
+    y = torch.rand((args.batch, 1, args.views, D), device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    with torch.no_grad():
+        fn = lambda: proj.filtered_backprojection(y, ang)   # noqa: E731
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.iters):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+    print(f"filtered_backprojection {args.micro} batch {args.batch}, {args.views} views: "
+          f"{a.elapsed_time(b) / args.iters:.3f} ms per call")
 
 
 def uneven_instances(dev, seed=2024, n=24):
@@ -701,7 +735,10 @@ def main():
     ap.add_argument("--micro", default=None,
                     choices=["para", "flat", "arc", "cone_flat", "cone_arc", "spiral", "uneven"],
                     help="time one operator on a bounded problem instead (see the module docstring)")
-    ap.add_argument("--op", default="proj", choices=["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"])
+    ap.add_argument("--op", default="proj",
+                    choices=["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw", "fbp"])
+    ap.add_argument("--size", type=int, default=0, help="--micro 2-D: image size (default 512)")
+    ap.add_argument("--dets", type=int, default=0, help="--micro 2-D: detector cells (default 736)")
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--views", type=int, default=720)
     ap.add_argument("--iters", type=int, default=3)

@@ -109,4 +109,74 @@ def fidelity_graph(module: FidelityModule, x: torch.Tensor, y: torch.Tensor, ste
     return graph
 
 
-__all__ = ["FidelityModule", "fidelity_graph", "pridediff_projector", "pridediff_views"]
+class GraphedFidelity:
+    """One application of a FidelityModule, x -> x - w * AT(A x - y), replayed
+    from a CUDA graph captured once: the data-consistency step of a sampling
+    loop, called between evaluations of a network that stays in stock
+    PyTorch (GaussianDiffusion.sample calls it through learn_block at every
+    step, model/pridediff.py:276-277).
+
+    The graph reads a static input and a static sinogram and writes a static
+    output; ``set_sino`` loads the measured sinogram once per sampling run and
+    each call copies x in, replays and returns a copy of the output.  The
+    module's weight is read by the graph where it lies, so loading another
+    weight in place needs no recapture."""
+
+    def __init__(self, module: FidelityModule, x_like: torch.Tensor, sino_like: torch.Tensor):
+        self.module = module
+        self.x = torch.zeros_like(x_like)
+        self.y = torch.zeros_like(sino_like)
+        with torch.no_grad():
+            module(self.x, self.y)   # warm-up: plans, tables and kernel attributes
+        torch.cuda.synchronize(self.x.device)
+        self.graph = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.x.device)
+        s.wait_stream(torch.cuda.current_stream(self.x.device))
+        with torch.no_grad(), torch.cuda.stream(s):
+            with torch.cuda.graph(self.graph, stream=s):
+                self.out = module(self.x, self.y)
+        torch.cuda.current_stream(self.x.device).wait_stream(s)
+
+    def set_sino(self, sino: torch.Tensor) -> None:
+        self.y.copy_(sino)
+
+    def __call__(self, x: torch.Tensor, sino=None, t=None) -> torch.Tensor:
+        self.x.copy_(x)
+        self.graph.replay()
+        return self.out.clone()
+
+
+def sample(denoise_fn, learn_block, img: torch.Tensor, sino: torch.Tensor, alphas: torch.Tensor,
+           steps: int = None):
+    """GaussianDiffusion.sample (model/pridediff.py:256-298): from t = steps
+    down to 1, x1 = learn_block(denoise_fn(img, t - 1), sino, max(t - 2, 0)),
+    then img <- img - q(x1, t - 1) + q(x1, t - 2) with q(x, s) = a_s x +
+    (1 - a_s) noise (q_sample, :300-305; the last step uses x1 itself).
+    `learn_block(x, sino, t)` carries the data-consistency step (a
+    GraphedFidelity inside it replays it from a CUDA graph).  Returns (the
+    input, the first step's reconstruction, the final image), as the
+    reference does."""
+    b = img.shape[0]
+    t = int(alphas.numel()) if steps is None else int(steps)
+    noise, xt, direct = img, img, None
+
+    def q(x, s):
+        a = alphas.gather(-1, s).reshape(b, *((1,) * (x.dim() - 1)))
+        return a * x + (1.0 - a) * noise
+
+    with torch.no_grad():
+        while t:
+            step = torch.full((b,), t - 1, dtype=torch.long, device=img.device)
+            step2 = torch.full((b,), max(t - 2, 0), dtype=torch.long, device=img.device)
+            x1 = learn_block(denoise_fn(img, step), sino, step2)
+            if direct is None:
+                direct = x1
+            xt_bar = q(x1, step)
+            xt_sub1 = q(x1, step2) if t - 1 != 0 else x1
+            img = img - xt_bar + xt_sub1
+            t -= 1
+    return xt, direct, img
+
+
+__all__ = ["FidelityModule", "GraphedFidelity", "fidelity_graph", "pridediff_projector", "pridediff_views",
+           "sample"]

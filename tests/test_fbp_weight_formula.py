@@ -52,3 +52,43 @@ def test_arc_weight_is_the_reciprocal_squared_distance(r, half):
     ref = (f32(1.0) / (a * a + b * b)).astype(np.float64)
     exact = 1.0 / ((a.astype(np.float64)) ** 2 + (b.astype(np.float64)) ** 2)
     assert (np.abs(ref - exact) / exact).max() <= 4 * 2.0 ** -24
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scan", ["flat", "arc"])
+def test_gpu_kernel_weight_against_fp64(scan):
+    """The weight as the CUDA kernels apply it: for one view and a sinogram of
+    ones, BackProjWeighted / BackProj at a pixel is that pixel's FBP weight
+    (flat: r^2 / (r - s.p / r)^2; arc: 1 / |s - p|^2, which the reference
+    divides by), up to the rounding of the two sums.  Compared with the FP64
+    formula at the FP32 source and pixel-centre coordinates the kernels use."""
+    import torch
+    from pridediff_gb300 import radontorch as RT
+    W = H = 64
+    pix, R, SDD, D = 2.6, 595.0, 1085.6, 200
+    det = 1.2858 / SDD if scan == "arc" else 1.2858
+    opt = torch.tensor([W, H, D, pix, pix, det, R, SDD, 0.0, 0.0, 0.0], dtype=torch.float32)
+    name = "FanFlat" if scan == "flat" else "FanArc"
+    worst = 0.0
+    for view in (0.3, 1.2, 2.9, 4.4, 5.95):
+        ang = torch.tensor([view], dtype=torch.float32, device="cuda")
+        ones = torch.ones((1, 1, 1, D), device="cuda")
+        bp = getattr(RT, f"BackProj{name}Dis2d")(ones, opt, ang)[0, 0].double().cpu().numpy()
+        bpw = getattr(RT, f"BackProjWeighted{name}Dis2d")(ones, opt, ang)[0, 0].double().cpu().numpy()
+        v32 = np.float32(view)
+        s, c = f32(np.sin(np.float64(v32))), f32(np.cos(np.float64(v32)))
+        sx, sy = float(f32(-s * f32(R))), float(f32(c * f32(R)))
+        cols = (np.arange(W) + 0.5) * pix - W / 2 * pix
+        rows = H / 2 * pix - (np.arange(H) + 0.5) * pix
+        px = cols.astype(f32).astype(np.float64)[None, :]
+        py = rows.astype(f32).astype(np.float64)[:, None]
+        if scan == "flat":
+            d = (sx * px + sy * py) / R
+            w = R * R / (R - d) ** 2
+        else:
+            w = 1.0 / ((sx - px) ** 2 + (sy - py) ** 2)
+        m = bp > 1e-3 * bp.max()
+        rel = np.abs(bpw[m] / bp[m] / w[m] - 1.0)
+        worst = max(worst, float(rel.max()))
+    print(f"{scan}: FBP weight as applied by the kernels vs FP64: {worst:.2e} relative")
+    assert worst <= 16 * 2.0 ** -24

@@ -75,3 +75,61 @@ def test_gpu_fidelity_graph_replays_the_eager_steps():
     graph.replay()
     torch.cuda.synchronize()
     assert rel_l2(xg.cpu().numpy(), xe.cpu().numpy()) <= 1e-6
+
+
+class _TinyDenoiser(torch.nn.Module):
+    """A small stock-PyTorch network standing in for PrideDiff's UNet."""
+
+    def __init__(self):
+        super().__init__()
+        self.c1 = torch.nn.Conv2d(1, 8, 3, padding=1)
+        self.c2 = torch.nn.Conv2d(8, 1, 3, padding=1)
+        self.t = torch.nn.Embedding(16, 8)
+
+    def forward(self, x, t):
+        h = torch.relu(self.c1(x) + self.t(t)[:, :, None, None])
+        return x + 0.1 * self.c2(h)
+
+
+class _LearnBlock(torch.nn.Module):
+    """PrideDiff's IterBlock (model/pridediff.py:137-151): relu(DC(x) + cnn(x))."""
+
+    def __init__(self, dc):
+        super().__init__()
+        self.dc = dc
+        self.cnn = torch.nn.Conv2d(1, 1, 3, padding=1)
+
+    def forward(self, x, sino, t):
+        return torch.relu(self.dc(x, sino, t) + 0.05 * self.cnn(x))
+
+
+@pytest.mark.gpu
+def test_gpu_sampling_loop_with_graph_captured_dc_matches_eager():
+    """GaussianDiffusion.sample's loop (model/pridediff.py:256-298) with a
+    stock-PyTorch denoiser, its learn block's data-consistency step replayed
+    from a CUDA graph at every step, equals the same loop run eagerly."""
+    from pridediff_gb300.fidelity import GraphedFidelity, sample
+    m, x, y = _small("exact")
+    torch.manual_seed(0)
+    den = _TinyDenoiser().cuda().eval()
+    steps = 10
+    alphas = torch.clip(1 - torch.linspace(0, steps, steps) / steps, 0, 0.999).cuda()
+    eager = _LearnBlock(m).cuda().eval()
+    with torch.no_grad():
+        sino = m.proj.projection(x, m.views)
+    g = GraphedFidelity(m, x, sino)
+    g.set_sino(sino)
+    graphed = _LearnBlock(g).cuda().eval()
+    graphed.cnn.load_state_dict(eager.cnn.state_dict())
+    _, d_e, out_e = sample(den, eager, x, sino, alphas)
+    _, d_g, out_g = sample(den, graphed, x, sino, alphas)
+    torch.cuda.synchronize()
+    assert rel_l2(d_g.cpu().numpy(), d_e.cpu().numpy()) <= 1e-6
+    assert rel_l2(out_g.cpu().numpy(), out_e.cpu().numpy()) <= 1e-6
+    # the graph replays the module's current weight: loading another one in place needs no recapture
+    with torch.no_grad():
+        m.weight.fill_(0.1)
+    _, _, out_e2 = sample(den, eager, x, sino, alphas)
+    _, _, out_g2 = sample(den, graphed, x, sino, alphas)
+    assert rel_l2(out_g2.cpu().numpy(), out_e2.cpu().numpy()) <= 1e-6
+    assert rel_l2(out_g2.cpu().numpy(), out_g.cpu().numpy()) > 1e-4

@@ -86,7 +86,7 @@ def test_config1_parallel_full(oracle_mod, op):
     assert e <= 1e-5
 
 
-@pytest.mark.parametrize("op", ["proj", "proj_t", "bproj", "bproj_t"])
+@pytest.mark.parametrize("op", ["proj", "proj_t", "bproj", "bproj_t", "bproj_w", "bproj_tw"])
 def test_config2_fanflat_full_size(oracle_mod, op):
     opt, ang = C2
     rng = np.random.default_rng(12)

@@ -151,3 +151,28 @@ def test_config3_uneven_24_instances_50_captured_steps():
     for _ in range(3):
         parts = [x - eta * p.projection_t(p.projection(x, a) - yy, a) for p, a, x, yy in zip(projs, angs, parts, ys)]
     assert rel_l2(ub.pack(parts).cpu().numpy(), xc.cpu().numpy()) <= 1e-5
+
+
+def test_uneven_24_instance_configuration_matches_reference_cpu(oracle_mod):
+    """Every instance of the 24-instance uneven configuration (image sizes
+    {256,384,512}^2, views {360,576,720}, detectors {368,512,736}; the draw
+    bench.py times), forward and exact adjoint through the persistent batch,
+    against the FP32 oracle (bit-exact with deeprecon's CPU path) at 1e-5."""
+    import bench
+    from pridediff_gb300.batch import UnevenBatch2d
+    dev = torch.device("cuda", 0)
+    projs, angs, imgs, _ = bench.uneven_instances(dev)
+    ub = UnevenBatch2d(projs, angs)
+    ys = ub.unpack_sinos(ub.forward(ub.pack(imgs)))
+    g = torch.Generator(device="cuda").manual_seed(9)
+    rs = [torch.randn(s, device="cuda", generator=g) for s in ub.sino_shapes]
+    bs = ub.unpack_images(ub.adjoint(ub.pack(rs)))
+    worst = 0.0
+    for p, a, x, y, r, b in zip(projs, angs, imgs, ys, rs, bs):
+        opt = p.options.cpu().numpy()
+        ang = a.cpu().numpy()
+        ef = rel_l2(y[:, 0].cpu().numpy(), oracle_mod.run2d("flat", "proj", x[:, 0].cpu().numpy(), ang, opt, "f", 16))
+        ea = rel_l2(b[:, 0].cpu().numpy(), oracle_mod.run2d("flat", "proj_t", r[:, 0].cpu().numpy(), ang, opt, "f", 16))
+        worst = max(worst, ef, ea)
+        assert ef <= 1e-5 and ea <= 1e-5, (p.image_size, a.numel(), opt[2], ef, ea)
+    print(f"24 uneven instances: worst rel-L2 vs reference CPU {worst:.2e}")
