@@ -715,6 +715,24 @@ def run_comparator_workloads(dev, flush, ev, ref):
     return res
 
 
+def _forward_tune_record(lib):
+    """The single-geometry forward shapes the autotuner chose in this run,
+    with the CTA shape each resolves to (slices per CTA, cluster size)."""
+    from pridediff_gb300 import autotune
+    from pridediff_gb300 import _native as N
+    out = []
+    for rec in autotune.chosen():
+        w, h = rec.get("image", [512, 512])
+        g = N.Geom2d(w, h, rec.get("dets", 736), 0.66, 0.66, 1.2858, 595.0, 1085.6, 0.0, 0.0, 0.0)
+        t = N.Tune2d()
+        t.fwd_slices = int(rec["choice"].get("fwd_slices", 0))
+        t.fwd_cluster = int(rec["choice"].get("fwd_cluster", 0))
+        sl, cl = N.ctypes.c_int(), N.ctypes.c_int()
+        lib.dd2d_fwd_shape(N.SCAN2D.get(rec.get("scan", "flat"), 1), g, t, N.ctypes.byref(sl), N.ctypes.byref(cl))
+        out.append({**rec, "slices_per_cta": sl.value, "ctas_per_view_cluster": cl.value})
+    return out
+
+
 def workload_config():
     return {"workload": "fan-flat DD FP + exact-adjoint BP with autograd, 16 x 512^2 slices, "
                         "720 views over 360 deg, 736 dets x 1.2858 mm, SID 595, SDD 1085.6",
@@ -908,6 +926,7 @@ def main():
                          "compulsory_frac": compulsory / (dom_ms / 1e3) / 1e9 / peak,
                          "incidences_per_s": 2.0 * world * B * V * 512 * 512 / (ms / 1e3)},
             "kernels": kern,
+            "tune": {"forward2d": _forward_tune_record(lib)},
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(x_host.numel() * 4 + y_host.numel() * 4),
                     "d2h_bytes_per_step": int(g_host.numel() * 4)},

@@ -137,12 +137,29 @@ typedef struct dd_instance2d {
     int batch;        /* slices sharing this geometry */
 } dd_instance2d;
 
-/* tuning of the persistent launches (chosen by the autotuner) */
+/* launch shapes chosen by the autotuner (pridediff_gb300/autotune.py); zero
+ * fields take the defaults.  No counterpart in the reference (its launch
+ * shape is fixed, BLOCK_DIM 256).  Persistent (uneven-batch) launches: */
 typedef struct dd_tune2d {
-    int ctas_per_sm;  /* persistent CTAs per SM (0 = as many as fit; capped at that) */
-    int lpt_order;    /* items longest-first (1) or in instance order (0) */
-    int reserved[6];
+    int ctas_per_sm;    /* persistent CTAs per SM (0 = as many as fit; capped at that) */
+    int lpt_order;      /* items longest-first (1) or in instance order (0) */
+    /* single-geometry forward (dd2d_apply_planned_tuned): */
+    int fwd_slices;     /* slices per CTA: 4 (default) or 2 */
+    int fwd_cluster;    /* CTAs sharing a view's walked lines, a cluster: 2 (default) or 1 */
+    /* persistent forward: */
+    int items_cluster;  /* CTAs sharing an item's walked lines: 1 (default) or 2 */
+    int reserved[3];
 } dd_tune2d;
+
+/* dd2d_apply_planned with the single-geometry forward's CTA shape taken from
+ * `tune` (fwd_slices, fwd_cluster; NULL = defaults). */
+int dd2d_apply_planned_tuned(int scan, int op, const dd_geom2d *g, const void *plan, const float *in,
+                             float *out, int batch, int num_view, void *workspace, size_t workspace_bytes,
+                             const dd_tune2d *tune, dd_stream_t stream);
+/* The forward CTA shape a tune resolves to on this geometry (slices per CTA,
+ * cluster size): 4 slices become 2 where their line tables would not fit in
+ * shared memory. */
+int dd2d_fwd_shape(int scan, const dd_geom2d *g, const dd_tune2d *tune, int *slices, int *cluster);
 
 size_t dd2d_batch_plan_bytes(int scan, const dd_instance2d *inst, int n);
 size_t dd2d_batch_workspace_bytes(int scan, const dd_instance2d *inst, int n);

@@ -97,7 +97,8 @@ class _Instance2d(ctypes.Structure):
 
 
 class _Tune2d(ctypes.Structure):
-    _fields_ = [("ctas_per_sm", ctypes.c_int), ("lpt_order", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+    _fields_ = [("ctas_per_sm", ctypes.c_int), ("lpt_order", ctypes.c_int), ("fwd_slices", ctypes.c_int),
+                ("fwd_cluster", ctypes.c_int), ("items_cluster", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class _Geom3d(ctypes.Structure):
@@ -143,6 +144,10 @@ def _declare(lib):
     lib.dd2d_apply_planned.argtypes = [i, i, g2, vp, vp, vp, i, i, vp, sz, vp]
     ip = ctypes.POINTER(_Instance2d)
     tp = ctypes.POINTER(_Tune2d)
+    lib.dd2d_apply_planned_tuned.restype = i
+    lib.dd2d_apply_planned_tuned.argtypes = [i, i, g2, vp, vp, vp, i, i, vp, sz, tp, vp]
+    lib.dd2d_fwd_shape.restype = i
+    lib.dd2d_fwd_shape.argtypes = [i, g2, tp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     lib.dd2d_dc_workspace_bytes.restype = sz
     lib.dd2d_dc_workspace_bytes.argtypes = [i, g2, i, i]
     lib.dd2d_dc_step.restype = i

@@ -1,4 +1,10 @@
-"""Project autotuner for the launch shapes of the persistent kernels.
+"""Project autotuner for the launch shapes of the kernels.
+
+Two problems are tuned: the single-geometry forward's CTA shape (slices per
+CTA and the size of the cluster that shares a view's walked lines --
+``tune_forward2d``, run by the radontorch operators on the first forward of a
+geometry and batch) and the persistent uneven batch's launch (CTAs per SM,
+item order, cluster size per item -- ``tune_batch_dc``).
 
 A tuning problem is a key (what is being run: scan type, instance shapes,
 GPU, driver, library version) and a list of candidate configurations; the
@@ -106,7 +112,15 @@ def recorded(key: str, path: Optional[str] = None) -> Dict[str, float]:
 # GPU problems
 # ---------------------------------------------------------------------------
 # ctas_per_sm 0: as many persistent CTAs as fit on an SM
-BATCH_CANDIDATES = [{"ctas_per_sm": c, "lpt_order": o} for c in (0, 2, 4) for o in (1, 0)]
+BATCH_CANDIDATES = [{"ctas_per_sm": c, "lpt_order": o, "items_cluster": k}
+                    for c in (0, 2, 4) for o in (1, 0) for k in (1, 2)]
+# single-geometry forward: slices per CTA x CTAs per view's cluster
+FORWARD2D_CANDIDATES = [{"fwd_slices": b, "fwd_cluster": c} for b in (4, 2) for c in (2, 1)]
+
+
+def enabled() -> bool:
+    """Autotuning of the single-geometry forward on first use (PRIDEDIFF_AUTOTUNE=0 turns it off)."""
+    return os.environ.get("PRIDEDIFF_AUTOTUNE", "1") != "0"
 
 
 def gpu_signature(device) -> dict:
@@ -141,3 +155,41 @@ def tune_batch_dc(batch, x, y, eta: float = 0.0, reps: int = 3, candidates=None,
                 describe={"kind": "batch2d_dc", "scan": batch.scan, "instances": len(shapes)})
     batch.set_tune(best)
     return best
+
+
+_forward_choice: Dict[str, dict] = {}   # in-process copy of the cache's choices
+_forward_about: Dict[str, dict] = {}    # what each key is
+
+
+def forward2d_key(scan: int, geom_fields: tuple, batch: int, views: int, device) -> str:
+    return make_key(kind="forward2d", scan=scan, geom=list(geom_fields), batch=batch, views=views,
+                    **gpu_signature(device))
+
+
+def tune_forward2d(key: str, run, reps: int = 3, path=None, about: Optional[dict] = None) -> dict:
+    """Pick the single-geometry forward's CTA shape for one (geometry, batch):
+    `run(cfg)` enqueues one forward with that shape on the current stream."""
+    import torch
+    if key in _forward_choice:
+        return _forward_choice[key]
+    _forward_about[key] = about or {}
+
+    def measure(cfg):
+        run(cfg)   # warm-up (kernel attributes)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            run(cfg)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
+
+    best = tune(key, FORWARD2D_CANDIDATES, measure, path=path, describe={"kind": "forward2d", **(about or {})})
+    _forward_choice[key] = best
+    return best
+
+
+def chosen() -> List[dict]:
+    """The forward shapes chosen in this process: what was tuned, the shape
+    picked and the time of every candidate (seconds per call)."""
+    return [{**_forward_about.get(k, {}), "choice": v, "trials": recorded(k)} for k, v in _forward_choice.items()]

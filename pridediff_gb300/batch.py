@@ -66,7 +66,9 @@ class UnevenBatch2d:
     def set_tune(self, tune: dict):
         self.tune.ctas_per_sm = int(tune.get("ctas_per_sm", 0))
         self.tune.lpt_order = int(tune.get("lpt_order", 1))
-        self.tune_dict = {"ctas_per_sm": self.tune.ctas_per_sm, "lpt_order": self.tune.lpt_order}
+        self.tune.items_cluster = int(tune.get("items_cluster", 1))
+        self.tune_dict = {"ctas_per_sm": self.tune.ctas_per_sm, "lpt_order": self.tune.lpt_order,
+                          "items_cluster": self.tune.items_cluster}
         if hasattr(self, "plan"):
             self._plan()
 

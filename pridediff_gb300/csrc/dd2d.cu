@@ -139,9 +139,9 @@ __global__ void k_dettab(int geom, int mode, const float *__restrict__ sino, int
 constexpr int kFwdImages = 4;
 constexpr int kFwdWarps = 8;
 
-// blockIdx.x = view * kFwdCluster + rank in the view's cluster.
-template <int GEOM, int WEIGHTED, int NPASS, int NW, int BI>
-__global__ void __cluster_dims__(kFwdCluster, 1, 1) __launch_bounds__(NW * 32)
+// blockIdx.x = view * CL + rank in the view's cluster of CL CTAs.
+template <int GEOM, int WEIGHTED, int NPASS, int NW, int BI, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NW * 32)
 k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ views,
       const float *__restrict__ dp, const float *__restrict__ bcoef,
       const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines,
@@ -149,12 +149,12 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
       const float *__restrict__ sub, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int rsmax = rs_entries(g.width > g.height ? g.width : g.height);
-    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, kFwdCluster, NW);
+    const FwdSmem L = fwd_smem(GEOM, g.num_det, rsmax, BI, CL, NW);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L.bar);
     init_bars(bar);
     DdPhases ph;
     FwdItem it;
-    it.v = blockIdx.x / kFwdCluster;
+    it.v = blockIdx.x / CL;
     it.b0 = blockIdx.y * BI;
     it.nb = min(BI, B - it.b0);
     it.V = V;
@@ -168,7 +168,7 @@ k_fwd(dd_geom2d g, int op, int B, int V, int nl, const DdView2 *__restrict__ vie
     it.taby = taby;
     it.out = out;
     it.sub = sub;
-    if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW, kFwdCluster>(g, op, it, smem, g.num_det, rsmax, ph) &&
+    if (!fwd_view<GEOM, WEIGHTED, NPASS, BI, NW, CL>(g, op, it, smem, g.num_det, rsmax, ph) &&
         threadIdx.x == 0)
         dd_report_timeout(status);
 }
@@ -556,41 +556,51 @@ int max_smem_optin() {
     return n;
 }
 
-template <int GEOM, int BI>
+template <int GEOM, int BI, int CL>
 static auto fwd_kernel(bool w, int D) {
     constexpr int NW = kFwdWarps;
-    auto kern = k_fwd<GEOM, 0, 8, NW, BI>;
+    auto kern = k_fwd<GEOM, 0, 8, NW, BI, CL>;
     switch (npass_class(D, NW)) {
-    case 1: kern = w ? k_fwd<GEOM, 1, 1, NW, BI> : k_fwd<GEOM, 0, 1, NW, BI>; break;
-    case 2: kern = w ? k_fwd<GEOM, 1, 2, NW, BI> : k_fwd<GEOM, 0, 2, NW, BI>; break;
-    case 3: kern = w ? k_fwd<GEOM, 1, 3, NW, BI> : k_fwd<GEOM, 0, 3, NW, BI>; break;
-    case 4: kern = w ? k_fwd<GEOM, 1, 4, NW, BI> : k_fwd<GEOM, 0, 4, NW, BI>; break;
-    default: kern = w ? k_fwd<GEOM, 1, 8, NW, BI> : k_fwd<GEOM, 0, 8, NW, BI>; break;
+    case 1: kern = w ? k_fwd<GEOM, 1, 1, NW, BI, CL> : k_fwd<GEOM, 0, 1, NW, BI, CL>; break;
+    case 2: kern = w ? k_fwd<GEOM, 1, 2, NW, BI, CL> : k_fwd<GEOM, 0, 2, NW, BI, CL>; break;
+    case 3: kern = w ? k_fwd<GEOM, 1, 3, NW, BI, CL> : k_fwd<GEOM, 0, 3, NW, BI, CL>; break;
+    case 4: kern = w ? k_fwd<GEOM, 1, 4, NW, BI, CL> : k_fwd<GEOM, 0, 4, NW, BI, CL>; break;
+    default: kern = w ? k_fwd<GEOM, 1, 8, NW, BI, CL> : k_fwd<GEOM, 0, 8, NW, BI, CL>; break;
     }
     return kern;
+}
+
+// The forward CTA shape a tune asks for (slices per CTA, CTAs per view's
+// cluster), with the defaults where it asks for none, and 2 slices where the
+// line tables of 4 would not fit in shared memory (lines of more than about
+// 3,400 pixels).
+static void fwd_shape(int geom, const dd_geom2d *g, const dd_tune2d *tune, int *bi, int *cl) {
+    const int rsmax = rs_entries(g->width > g->height ? g->width : g->height);
+    *bi = (tune && (tune->fwd_slices == 2 || tune->fwd_slices == 4)) ? tune->fwd_slices : kFwdImages;
+    *cl = (tune && (tune->fwd_cluster == 1 || tune->fwd_cluster == 2)) ? tune->fwd_cluster : kFwdCluster;
+    if (*bi == 4 && fwd_smem(geom, g->num_det, rsmax, 4, *cl, kFwdWarps).total > max_smem_optin()) *bi = 2;
 }
 
 template <int GEOM>
 static int launch_fwd(int op, const dd_geom2d *g, const PlanLayout &P, const char *planb, int B,
                       int V, const float2 *tx, const float2 *ty, float *out, const float *sub,
-                      int *status, cudaStream_t st) {
+                      int *status, cudaStream_t st, const dd_tune2d *tune) {
     const int rsmax = rs_entries(g->width > g->height ? g->width : g->height);
     const bool w = (op == DD_OP_BPROJ_TW);
-    // 4 images per CTA; 2 where the line tables of 4 would not fit in shared
-    // memory (lines of more than about 3,400 pixels)
     constexpr int NW = kFwdWarps;
-    const int bi = fwd_smem(GEOM, g->num_det, rsmax, kFwdImages, kFwdCluster, NW).total <= max_smem_optin()
-                       ? kFwdImages : 2;
-    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, kFwdCluster, NW);
+    int bi, cl;
+    fwd_shape(GEOM, g, tune, &bi, &cl);
+    const FwdSmem S = fwd_smem(GEOM, g->num_det, rsmax, bi, cl, NW);
     if (S.total > max_smem_optin()) return DD_ERR_SIZE_OVERFLOW;
-    if ((long long)V * kFwdCluster > 0x7FFFFFFFLL) return DD_ERR_SIZE_OVERFLOW;
-    dim3 grid(V * kFwdCluster, (B + bi - 1) / bi);
+    if ((long long)V * cl > 0x7FFFFFFFLL) return DD_ERR_SIZE_OVERFLOW;
+    dim3 grid(V * cl, (B + bi - 1) / bi);
     const DdView2 *views = (const DdView2 *)(planb + P.views);
     const float *dp = (const float *)(planb + P.dp);
     const float *bc = (const float *)(planb + P.bcoef);
     const DdLine *lines = (const DdLine *)(planb + P.lines);
     const DdLine *dlines = GEOM == DD_GEOM_PARA ? (const DdLine *)(planb + P.dlines) : nullptr;
-    auto kern = (bi == kFwdImages) ? fwd_kernel<GEOM, kFwdImages>(w, g->num_det) : fwd_kernel<GEOM, 2>(w, g->num_det);
+    auto kern = (bi == 4) ? (cl == 2 ? fwd_kernel<GEOM, 4, 2>(w, g->num_det) : fwd_kernel<GEOM, 4, 1>(w, g->num_det))
+                          : (cl == 2 ? fwd_kernel<GEOM, 2, 2>(w, g->num_det) : fwd_kernel<GEOM, 2, 1>(w, g->num_det));
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
@@ -680,7 +690,8 @@ int launch_det_tables(int geom, int op, const dd_geom2d *g, const char *planb, c
 
 int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const float *in,
                   float *out, int B, int V, void *ws, size_t wsb, cudaStream_t st,
-                  const float *sub = nullptr, const float *base = nullptr, float scale = 1.0f) {
+                  const float *sub = nullptr, const float *base = nullptr, float scale = 1.0f,
+                  const dd_tune2d *tune = nullptr) {
     const PlanLayout P = plan_layout(scan, g, V);
     const float *angles = (const float *)((const char *)planp + P.ang);
     const ApplyLayout A = apply_layout(op, g, B, V);
@@ -695,9 +706,9 @@ int apply_planned(int scan, int op, const dd_geom2d *g, const void *planp, const
         const int ts = launch_image_tables(g, in, B, tx, ty, st);
         if (ts != DD_OK) return ts;
         if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;
-        if (geom == DD_GEOM_PARA) return launch_fwd<DD_GEOM_PARA>(op, g, P, planb, B, V, tx, ty, out, sub, status, st);
-        if (geom == DD_GEOM_FLAT) return launch_fwd<DD_GEOM_FLAT>(op, g, P, planb, B, V, tx, ty, out, sub, status, st);
-        return launch_fwd<DD_GEOM_ARC>(op, g, P, planb, B, V, tx, ty, out, sub, status, st);
+        if (geom == DD_GEOM_PARA) return launch_fwd<DD_GEOM_PARA>(op, g, P, planb, B, V, tx, ty, out, sub, status, st, tune);
+        if (geom == DD_GEOM_FLAT) return launch_fwd<DD_GEOM_FLAT>(op, g, P, planb, B, V, tx, ty, out, sub, status, st, tune);
+        return launch_fwd<DD_GEOM_ARC>(op, g, P, planb, B, V, tx, ty, out, sub, status, st, tune);
     }
     float2 *dtab = (float2 *)(wb + A.dtab);
     const int ts = launch_det_tables(geom, op, g, planb, in, B, V, dtab, st);
@@ -770,6 +781,23 @@ extern "C" int dd2d_apply_planned(int scan, int op, const dd_geom2d *g, const vo
     if (st != DD_OK) return st;
     return apply_planned(scan, op, g, planp, in, out, batch, num_view, workspace, workspace_bytes,
                          (cudaStream_t)stream);
+}
+
+extern "C" int dd2d_apply_planned_tuned(int scan, int op, const dd_geom2d *g, const void *planp,
+                                        const float *in, float *out, int batch, int num_view,
+                                        void *workspace, size_t workspace_bytes, const dd_tune2d *tune,
+                                        dd_stream_t stream) {
+    ddtrace::Range tr("dd2d_apply_planned", scan, op, false);
+    const int st = validate(scan, op, g, batch, num_view);
+    if (st != DD_OK) return st;
+    return apply_planned(scan, op, g, planp, in, out, batch, num_view, workspace, workspace_bytes,
+                         (cudaStream_t)stream, nullptr, nullptr, 1.0f, tune);
+}
+
+extern "C" int dd2d_fwd_shape(int scan, const dd_geom2d *g, const dd_tune2d *tune, int *slices, int *cluster) {
+    if (!g || !slices || !cluster || scan < DD_SCAN_PARA || scan > DD_SCAN_ARC) return DD_ERR_INVALID_ARG;
+    fwd_shape(geom_of(scan), g, tune, slices, cluster);
+    return DD_OK;
 }
 
 extern "C" size_t dd2d_dc_workspace_bytes(int scan, const dd_geom2d *g, int batch, int num_view) {

@@ -198,16 +198,18 @@ __host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <
 // single-geometry forward's cluster as two interleaved halves, so the two
 // projections of an instance agree to FP32 rounding, not bit for bit
 // (walking the lines in the cluster's order cost 8.73 vs 8.13 ms).
+// The cluster size is a tuning choice (dd_tune2d.items_cluster): 1 unless the
+// autotuner finds 2 faster for the batch at hand.
 constexpr int kFwdItemsCluster = 1;
 
-template <int GEOM, int NPASS>
-__global__ void __cluster_dims__(kFwdItemsCluster, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
+template <int GEOM, int NPASS, int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
 k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
             float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, kFwdItemsCluster);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, CL);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
     // the item and its geometry live in shared memory: read where used, they
     // hold no registers across the line loop (the plain forward reads them
@@ -217,7 +219,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
     DdPhases ph;
     for (;;) {
         int i;
-        if constexpr (kFwdItemsCluster > 1) i = next_item_cluster(counter);
+        if constexpr (CL > 1) i = next_item_cluster(counter);
         else i = next_item(counter);
         if (i >= nitems) break;
         if (threadIdx.x == 0) {
@@ -243,7 +245,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
             s_g = d.g;
         }
         __syncthreads();   // every thread passed the cluster barrier above before s_it changes
-        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, kFwdItemsCluster>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
+        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, CL>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) dd_report_timeout(status);
             break;
         }
@@ -369,22 +371,30 @@ static int cluster_grid_of(const dd_tune2d *t, int nitems, K kern, int smem, int
     return clusters * cl;
 }
 
+template <int GEOM, int CL>
+static auto fwd_items_kernel(int Dmax) {
+    auto kern = k_fwd_items<GEOM, 8, CL>;
+    switch (npass_class(Dmax)) {
+    case 1: kern = k_fwd_items<GEOM, 1, CL>; break;
+    case 2: kern = k_fwd_items<GEOM, 2, CL>; break;
+    case 3: kern = k_fwd_items<GEOM, 3, CL>; break;
+    case 4: kern = k_fwd_items<GEOM, 4, CL>; break;
+    default: break;
+    }
+    return kern;
+}
+
 template <int GEOM>
 static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, const float2 *tabs,
                             float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
-    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, kFwdItemsCluster);
-    auto kern = k_fwd_items<GEOM, 8>;
-    switch (npass_class(L.Dmax)) {
-    case 1: kern = k_fwd_items<GEOM, 1>; break;
-    case 2: kern = k_fwd_items<GEOM, 2>; break;
-    case 3: kern = k_fwd_items<GEOM, 3>; break;
-    case 4: kern = k_fwd_items<GEOM, 4>; break;
-    default: break;
-    }
+    int cl = (tune && tune->items_cluster == 2) ? 2 : kFwdItemsCluster;
+    if (cl == 2 && fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, 2).total > max_smem_optin()) cl = 1;
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, cl);
+    auto kern = (cl == 2) ? fwd_items_kernel<GEOM, 2>(L.Dmax) : fwd_items_kernel<GEOM, 1>(L.Dmax);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
-    const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, kFwdItemsCluster);
+    const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, cl);
     ProfRec *pr = prof_begin(DD_KERNEL_FORWARD, st);
     kern<<<grid, kThreads, S.total, st>>>(op, (const BatchInst *)(planb + L.desc),
                                           (const int4 *)(planb + L.fitems), L.nfwd, planb, L.plans, tabs,

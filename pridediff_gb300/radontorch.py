@@ -151,10 +151,46 @@ def _apply2d(scan: str, op: str, x: torch.Tensor, options, angles: torch.Tensor)
         plan = plan2d(scan, g, angles)
         nbytes = int(lib.dd2d_apply_workspace_bytes(sc, opc, g, B * C, V))
         ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=x.device)
-        st = lib.dd2d_apply_planned(sc, opc, g, plan.data_ptr(), x.data_ptr(), out.data_ptr(), B * C, V,
-                                    ws.data_ptr(), nbytes, _stream_ptr(x.device))
+
+        def run(cfg):
+            return lib.dd2d_apply_planned_tuned(sc, opc, g, plan.data_ptr(), x.data_ptr(), out.data_ptr(), B * C,
+                                                V, ws.data_ptr(), nbytes, forward_tune(cfg),
+                                                _stream_ptr(x.device))
+        cfg = forward_shape(sc, g, B * C, V, x.device, run) if image_in else None
+        st = run(cfg)
     N.check(st, f"{scan} {op}")
     return out
+
+
+def forward_tune(cfg):
+    """dd_tune2d for a forward shape {fwd_slices, fwd_cluster} (None: defaults)."""
+    t = N.Tune2d()
+    if cfg:
+        t.fwd_slices = int(cfg.get("fwd_slices", 0))
+        t.fwd_cluster = int(cfg.get("fwd_cluster", 0))
+    return t
+
+
+def forward_shape(sc: int, g, batch: int, views: int, device, run):
+    """The single-geometry forward's CTA shape for this geometry and batch,
+    chosen by the autotuner on first use (timing every candidate on the
+    call's own buffers, which the chosen shape then overwrites) and kept for
+    the process and in the tuner's cache; the library's defaults while a
+    stream is being captured or when tuning is off (PRIDEDIFF_AUTOTUNE=0)."""
+    from . import autotune
+    if not autotune.enabled():
+        return None
+    key = autotune.forward2d_key(sc, tuple(getattr(g, f) for f, _ in g._fields_), batch, views, device)
+    if key in autotune._forward_choice:
+        return autotune._forward_choice[key]
+    if torch.cuda.is_current_stream_capturing():
+        return None
+
+    def launch(cfg):
+        N.check(run(cfg), "forward tuning")
+    about = {"scan": {v: k for k, v in N.SCAN2D.items()}[sc], "image": [g.width, g.height], "dets": g.num_det,
+             "views": views, "batch": batch}
+    return autotune.tune_forward2d(key, launch, about=about)
 
 
 def plan3d(scan: str, g, angles: torch.Tensor, source_pos=None):
