@@ -8,9 +8,14 @@ forward projection, the exact adjoint, or the DC step
 kernel launch per operator, work items pulled longest-first from a device
 counter (``libpridediff_dd.so``: dd2d_batch_*).
 
-Tensors are packed instance after instance (flat float32 tensors); ``pack``
-and ``unpack`` convert from/to lists of (batch_i, 1, H_i, W_i) images or
-(batch_i, 1, V_i, D_i) sinograms.
+Tensors are packed into flat float32 tensors; ``pack`` and ``unpack_*``
+convert from/to lists of (batch_i, 1, H_i, W_i) images or (batch_i, 1, V_i,
+D_i) sinograms, one per instance in the order given.  Instances with the same
+geometry and the same view angles are merged into one multi-slice instance
+(``group=True``, the default): their slices then share each work item's
+per-line set-up and each adjoint-map block read, and the packed layout keeps
+a group's slices together (``pack`` / ``unpack_*`` apply that order).  Merging
+changes no arithmetic: every slice's result is the same bit for bit.
 
 ``dc_graph`` captures ``steps`` DC steps in one CUDA graph: replaying it
 launches no host work at all.  The reference runs each step as separate
@@ -31,7 +36,7 @@ from .radontorch import host_options
 
 class UnevenBatch2d:
     def __init__(self, projectors: Sequence, angles: Sequence[torch.Tensor],
-                 batch: Optional[Sequence[int]] = None, tune: Optional[dict] = None):
+                 batch: Optional[Sequence[int]] = None, tune: Optional[dict] = None, group: bool = True):
         if len(projectors) == 0 or len(projectors) != len(angles):
             raise ValueError("need one angles tensor per projector")
         scans = {p.scan_type for p in projectors}
@@ -46,18 +51,34 @@ class UnevenBatch2d:
         if any(a.device != self.device or a.dtype != torch.float32 for a in self.angles):
             raise RuntimeError("angles must be float32 tensors on one CUDA device")
         self.batch = list(batch) if batch is not None else [1] * len(projectors)
-        n = len(projectors)
-        self.n = n
         self.geoms = [N.geom2d(host_options(p.options)) for p in projectors]
-        self.inst = (N.Instance2d * n)()
-        for i, (g, a, b) in enumerate(zip(self.geoms, self.angles, self.batch)):
-            self.inst[i].geom = g
-            self.inst[i].num_view = int(a.shape[0])
-            self.inst[i].batch = int(b)
         self.img_shapes = [(b, 1, g.height, g.width) for g, b in zip(self.geoms, self.batch)]
         self.sino_shapes = [(b, 1, int(a.shape[0]), g.num_det) for g, a, b in zip(self.geoms, self.angles, self.batch)]
         self.img_numel = sum(s[0] * s[2] * s[3] for s in self.img_shapes)
         self.sino_numel = sum(s[0] * s[2] * s[3] for s in self.sino_shapes)
+        # groups of instances with the same geometry and angles, in order of first appearance
+        self.groups: List[List[int]] = []
+        keys = []
+        for i, (g, a) in enumerate(zip(self.geoms, self.angles)):
+            key = tuple(getattr(g, f) for f, _ in g._fields_) + (int(a.shape[0]),)
+            for gi, k in enumerate(keys):
+                if group and k == key and torch.equal(self.angles[self.groups[gi][0]], a):
+                    self.groups[gi].append(i)
+                    break
+            else:
+                keys.append(key)
+                self.groups.append([i])
+        n = len(self.groups)
+        self.n = n
+        self.inst = (N.Instance2d * n)()
+        for gi, members in enumerate(self.groups):
+            i0 = members[0]
+            self.inst[gi].geom = self.geoms[i0]
+            self.inst[gi].num_view = int(self.angles[i0].shape[0])
+            self.inst[gi].batch = sum(int(self.batch[i]) for i in members)
+        self._order = [i for members in self.groups for i in members]   # packed order of the instances
+        self._img_off = self._offsets(self.img_shapes)
+        self._sino_off = self._offsets(self.sino_shapes)
         self.tune = N.Tune2d()
         self.set_tune(tune or {})
         self._plan()
@@ -79,7 +100,7 @@ class UnevenBatch2d:
             N.check(lib.dd2d_validate(self.sc, N.OPS["proj"], ctypes.byref(self.geoms[0]), 1, 1) or
                     N.DD_ERR_INVALID_ARG, "uneven batch")
         self.plan = torch.empty(nb, dtype=torch.uint8, device=self.device)
-        ptrs = (ctypes.c_void_p * self.n)(*[a.data_ptr() for a in self.angles])
+        ptrs = (ctypes.c_void_p * self.n)(*[self.angles[m[0]].data_ptr() for m in self.groups])
         with torch.cuda.device(self.device):
             N.check(lib.dd2d_batch_plan(self.sc, self.inst, self.n, ptrs, self.plan.data_ptr(), nb,
                                         ctypes.byref(self.tune), self._stream()), "uneven batch plan")
@@ -90,24 +111,26 @@ class UnevenBatch2d:
         return torch.cuda.current_stream(self.device).cuda_stream
 
     # -- packing ---------------------------------------------------------------
+    def _offsets(self, shapes):
+        """Offset of each instance's block in the packed order."""
+        off, o = [0] * len(shapes), 0
+        for i in self._order:
+            off[i] = o
+            o += shapes[i][0] * shapes[i][2] * shapes[i][3]
+        return off
+
     def pack(self, xs: List[torch.Tensor]) -> torch.Tensor:
-        return torch.cat([x.reshape(-1) for x in xs]).contiguous()
+        """One flat tensor from per-instance images (or sinograms), in the packed order."""
+        return torch.cat([xs[i].reshape(-1) for i in self._order]).contiguous()
+
+    def _unpack(self, flat, shapes, off):
+        return [flat[o:o + s[0] * s[2] * s[3]].view(s) for s, o in zip(shapes, off)]
 
     def unpack_images(self, flat: torch.Tensor) -> List[torch.Tensor]:
-        out, o = [], 0
-        for s in self.img_shapes:
-            k = s[0] * s[2] * s[3]
-            out.append(flat[o:o + k].view(s))
-            o += k
-        return out
+        return self._unpack(flat, self.img_shapes, self._img_off)
 
     def unpack_sinos(self, flat: torch.Tensor) -> List[torch.Tensor]:
-        out, o = [], 0
-        for s in self.sino_shapes:
-            k = s[0] * s[2] * s[3]
-            out.append(flat[o:o + k].view(s))
-            o += k
-        return out
+        return self._unpack(flat, self.sino_shapes, self._sino_off)
 
     # -- operators -------------------------------------------------------------
     def _apply(self, op: str, x: torch.Tensor) -> torch.Tensor:

@@ -176,3 +176,30 @@ def test_uneven_24_instance_configuration_matches_reference_cpu(oracle_mod):
         worst = max(worst, ef, ea)
         assert ef <= 1e-5 and ea <= 1e-5, (p.image_size, a.numel(), opt[2], ef, ea)
     print(f"24 uneven instances: worst rel-L2 vs reference CPU {worst:.2e}")
+
+
+def test_instances_with_one_geometry_are_merged_without_changing_results():
+    """Instances with the same geometry and angles become one multi-slice
+    instance; every slice's forward and adjoint stay bit-identical."""
+    import pridediff_gb300 as P
+    from pridediff_gb300.batch import UnevenBatch2d
+    sizes = [(256, 360, 368), (384, 576, 512), (256, 360, 368), (512, 360, 368), (384, 576, 512), (256, 360, 368)]
+    projs = [P.projector2d(n, D, FAN["pix"], FAN["det"], FAN["sid"], FAN["sdd"], scan_type="flat").cuda()
+             for n, _, D in sizes]
+    angs = [torch.arange(V, dtype=torch.float32, device="cuda") * (2 * np.pi / V) for _, V, _ in sizes]
+    batch = [1, 2, 1, 1, 1, 2]
+    merged = UnevenBatch2d(projs, angs, batch)
+    plain = UnevenBatch2d(projs, angs, batch, group=False)
+    assert merged.n == 3 and plain.n == 6
+    assert merged.groups == [[0, 2, 5], [1, 4], [3]]
+    xs = _rand_images(projs, batch, 21)
+    fm = merged.unpack_sinos(merged.forward(merged.pack(xs)))
+    fp = plain.unpack_sinos(plain.forward(plain.pack(xs)))
+    for a, b in zip(fm, fp):
+        assert torch.equal(a, b)
+    g = torch.Generator(device="cuda").manual_seed(22)
+    rs = [torch.randn(s, device="cuda", generator=g) for s in plain.sino_shapes]
+    am = merged.unpack_images(merged.adjoint(merged.pack(rs)))
+    ap = plain.unpack_images(plain.adjoint(plain.pack(rs)))
+    for a, b in zip(am, ap):
+        assert torch.equal(a, b)
