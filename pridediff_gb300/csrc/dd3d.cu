@@ -41,7 +41,6 @@ constexpr int kThreads = 256;
 constexpr int kNB = 2;     // volumes per thread
 constexpr int kTile = 16;  // adjoint: 16 x 16 voxel columns per CTA
 constexpr int kZS = 8;     // adjoint: slices per thread
-constexpr int kWarps3 = kThreads / 32;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -230,7 +229,12 @@ __global__ void __launch_bounds__(128) k_sino3(dd_geom3d g, const char *__restri
 // Forward-type kernel: detector gathers
 // ---------------------------------------------------------------------------
 constexpr int kFC = 32;    // detector columns per CTA (the lanes of a warp)
-constexpr int kFR = 8;     // consecutive detector rows per thread; 8 warps -> 64 rows per CTA
+// Forward CTA: 16 warps x 4 consecutive detector rows per thread = 64 rows,
+// 2 CTAs per SM at 64 registers.  (8 warps x 8 rows at 80 registers and 3
+// CTAs per SM: 5 to 8 % slower, the row loop spilling.)
+constexpr int kFR = 4;
+constexpr int kFwdThreads3 = 512;
+constexpr int kFwdWarps3 = kFwdThreads3 / 32;
 constexpr int kSeg = 8;    // column segments of one line held in shared memory
 
 struct Fwd3Args {
@@ -246,13 +250,13 @@ struct Fwd3Args {
 };
 
 // grid: (view, group of 32 columns inside one walk block, row block x volume
-// group).  Lane = column, warp w = rows r0 + 8w .. r0 + 8w + 7, kNB volumes.
+// group).  Lane = column, warp w = rows r0 + 4w .. r0 + 4w + 3, kNB volumes.
 // The overlap segments of a line (pixel, width x operator factor) depend on
 // the column only, so they are computed once per line and column -- by one
 // warp, in rotation, one line ahead -- into shared memory, and reused by all
 // 64 rows.  Line records arrive by bulk copies (TMA) two lines ahead.
 template <int GEOM, int FAMILY>
-__global__ void __launch_bounds__(kThreads, 3) k_fwd3(const Fwd3Args a) {
+__global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
     const int v = blockIdx.x, cg = blockIdx.y;
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd3(const Fwd3Args a) {
     const int cc = (cg * kFC) / DD3_CHUNK, c0 = cc * DD3_CHUNK;
     const int k = cg * kFC + lane, kk = k - c0;
     const bool active = k < C;
-    const int r0 = rb * (kFR * kWarps3) + warp * kFR, b0 = bg * kNB;
+    const int r0 = rb * (kFR * kFwdWarps3) + warp * kFR, b0 = bg * kNB;
     const int nb = min(kNB, a.B - b0);
     const PlanLayout &P = a.P;
 
@@ -364,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_fwd3(const Fwd3Args a) {
     if (tid == 0 && !abort_flag && nline > 2) issue(2, 0);
     for (int line = 0; line < nline && !abort_flag; line++) {
         const int sb = line & 1;
-        if (line + 1 < nline && warp == (line & (kWarps3 - 1)) && !produce(line + 1, sb ^ 1)) abort_flag = 1;
+        if (line + 1 < nline && warp == (line & (kFwdWarps3 - 1)) && !produce(line + 1, sb ^ 1)) abort_flag = 1;
         // consume line `line`
         const int n = segn[sb][lane];
         if (active && n > 0) {
@@ -776,9 +780,9 @@ int launch_fwd(int family, const Fwd3Args &a, cudaStream_t st) {
     const dim3 grid((unsigned)a.V, (unsigned)((a.g.num_col + kFC - 1) / kFC),
                     (unsigned)(a.nrb * ((a.B + kNB - 1) / kNB)));
     dd2::ProfRec *pr = dd2::prof_begin(DD_KERNEL_FORWARD, st);
-    if (family == 0) k_fwd3<GEOM, 0><<<grid, kThreads, 0, st>>>(a);
-    else if (family == 1) k_fwd3<GEOM, 1><<<grid, kThreads, 0, st>>>(a);
-    else k_fwd3<GEOM, 2><<<grid, kThreads, 0, st>>>(a);
+    if (family == 0) k_fwd3<GEOM, 0><<<grid, kFwdThreads3, 0, st>>>(a);
+    else if (family == 1) k_fwd3<GEOM, 1><<<grid, kFwdThreads3, 0, st>>>(a);
+    else k_fwd3<GEOM, 2><<<grid, kFwdThreads3, 0, st>>>(a);
     dd2::prof_end(pr, st);
     dd2::count_launches(1);
     return launch_status();
@@ -842,7 +846,7 @@ int forward(int scan, int op, const dd_geom3d *g, const char *planb, const float
     a.sub = sub;
     a.B = B;
     a.V = V;
-    a.nrb = (g->num_row + kFR * kWarps3 - 1) / (kFR * kWarps3);
+    a.nrb = (g->num_row + kFR * kFwdWarps3 - 1) / (kFR * kFwdWarps3);
     const int fam = op_family(op), geom = geom_of(scan);
     if (geom == DD_GEOM3_CONE_FLAT) return launch_fwd<DD_GEOM3_CONE_FLAT>(fam, a, st);
     if (geom == DD_GEOM3_CONE_ARC) return launch_fwd<DD_GEOM3_CONE_ARC>(fam, a, st);
