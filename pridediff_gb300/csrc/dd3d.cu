@@ -229,12 +229,12 @@ __global__ void __launch_bounds__(128) k_sino3(dd_geom3d g, const char *__restri
 // Forward-type kernel: detector gathers
 // ---------------------------------------------------------------------------
 constexpr int kFC = 32;    // detector columns per CTA (the lanes of a warp)
-// Forward CTA: 16 warps x 4 consecutive detector rows per thread = 64 rows,
-// 2 CTAs per SM at 64 registers.  (8 warps x 8 rows at 80 registers and 3
-// CTAs per SM: 5 to 8 % slower, the row loop spilling.)
+// Forward CTA: 8 consumer warps x 4 consecutive detector rows per thread =
+// 32 rows, plus a producer warp that turns each line's record into column
+// segments one line ahead; 3 CTAs per SM at 72 registers.
 constexpr int kFR = 4;
-constexpr int kFwdThreads3 = 512;
-constexpr int kFwdWarps3 = kFwdThreads3 / 32;
+constexpr int kFwdWarps3 = 8;                          // consumer warps
+constexpr int kFwdThreads3 = (kFwdWarps3 + 1) * 32;   // + the producer warp
 constexpr int kSeg = 8;    // column segments of one line held in shared memory
 
 struct Fwd3Args {
@@ -250,13 +250,14 @@ struct Fwd3Args {
 };
 
 // grid: (view, group of 32 columns inside one walk block, row block x volume
-// group).  Lane = column, warp w = rows r0 + 4w .. r0 + 4w + 3, kNB volumes.
-// The overlap segments of a line (pixel, width x operator factor) depend on
-// the column only, so they are computed once per line and column -- by one
-// warp, in rotation, one line ahead -- into shared memory, and reused by all
-// 64 rows.  Line records arrive by bulk copies (TMA) two lines ahead.
+// group).  Lane = column, consumer warp w = rows r0 + 4w .. r0 + 4w + 3, kNB
+// volumes.  The overlap segments of a line (pixel, width x operator factor)
+// depend on the column only, so they are computed once per line and column
+// -- by the producer warp, one line ahead, while the consumer warps walk the
+// current line -- into shared memory, and reused by all 32 rows.  Line
+// records arrive by bulk copies (TMA) two lines ahead.
 template <int GEOM, int FAMILY>
-__global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
+__global__ void __launch_bounds__(kFwdThreads3, 3) k_fwd3(const Fwd3Args a) {
     const dd_geom3d &g = a.g;
     const int W = g.width, H = g.height, Dp = g.depth, C = g.num_col, R = g.num_row;
     const int v = blockIdx.x, cg = blockIdx.y;
@@ -265,6 +266,7 @@ __global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
     const int cc = (cg * kFC) / DD3_CHUNK, c0 = cc * DD3_CHUNK;
     const int k = cg * kFC + lane, kk = k - c0;
     const bool active = k < C;
+    const bool prod = warp == kFwdWarps3;   // the producer warp owns no rows
     const int r0 = rb * (kFR * kFwdWarps3) + warp * kFR, b0 = bg * kNB;
     const int nb = min(kNB, a.B - b0);
     const PlanLayout &P = a.P;
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
 #pragma unroll
         for (int q = 0; q < kFR; q++) {
             const int r = r0 + q;
-            if (active && r < R) {
+            if (active && !prod && r < R) {
                 dd3_rp(GEOM, &w, mag, rz[2 * r], rz[2 * r + 1], &rp0[q], &rp1[q]);
             } else {
                 rp0[q] = 3.0e38f;    // empty row: the z walk never starts
@@ -363,15 +365,15 @@ __global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
         if (nline > 1) issue(1, 1);
     }
     __syncthreads();
-    if (warp == 0 && !produce(0, 0)) abort_flag = 1;
+    if (prod && !produce(0, 0)) abort_flag = 1;
     __syncthreads();
     if (tid == 0 && !abort_flag && nline > 2) issue(2, 0);
     for (int line = 0; line < nline && !abort_flag; line++) {
         const int sb = line & 1;
-        if (line + 1 < nline && warp == (line & (kFwdWarps3 - 1)) && !produce(line + 1, sb ^ 1)) abort_flag = 1;
+        if (line + 1 < nline && prod && !produce(line + 1, sb ^ 1)) abort_flag = 1;
         // consume line `line`
         const int n = segn[sb][lane];
-        if (active && n > 0) {
+        if (active && !prod && n > 0) {
             const float4 lz = slz[sb];
             const float *__restrict__ lsrc = src + (size_t)line * npix;
             if (n <= kSeg) {
@@ -441,7 +443,7 @@ __global__ void __launch_bounds__(kFwdThreads3, 2) k_fwd3(const Fwd3Args a) {
         }
         return;
     }
-    if (!active) return;
+    if (!active || prod) return;
     const int ko = w.flip ? C - 1 - k : k;
 #pragma unroll
     for (int q = 0; q < kFR; q++) {
