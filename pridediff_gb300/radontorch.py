@@ -74,30 +74,56 @@ def _stream_ptr(dev):
     return torch.cuda.current_stream(dev).cuda_stream
 
 
+def _plan_budget() -> int:
+    import os
+    return int(os.environ.get("PRIDEDIFF_PLAN_CACHE_BYTES", str(16 << 30)))
+
+
 class _PlanCache:
     """Geometry plans keyed by (scan, geometry, angles tensor identity/version).
 
-    A plan holds the per-view detector tables and the per-line drift pieces;
-    it depends only on the geometry and the angles, so iterative callers (the
-    data-consistency loop, autograd forward + backward) build it once.  The
-    entry keeps a weak reference to the angles tensor so a new tensor that
-    happens to reuse the same memory is never mistaken for the old one.
+    A plan holds the per-view detector tables, the per-line drift pieces and,
+    for fan beams, the adjoint map (about 1.8 GB for 512^2 pixels and 720
+    views); it depends only on the geometry and the angles, so iterative
+    callers (the data-consistency loop, autograd forward + backward) build it
+    once -- as long as they pass the same angles tensor: the key is the
+    tensor's identity and version, never its values (reading them would
+    synchronise), so an angles tensor rebuilt every call (a fresh
+    torch.arange) rebuilds the plan every call.  The entry keeps a weak
+    reference to the angles tensor so a new tensor that happens to reuse the
+    same memory is never mistaken for the old one.
+
+    At most `size` plans and `budget` bytes of them are kept (least recently
+    used first out; the newest plan is always kept); the byte budget defaults
+    to 16 GiB (PRIDEDIFF_PLAN_CACHE_BYTES).  `nbytes()` reports what is held,
+    `clear()` releases it.
     """
 
-    def __init__(self, size: int = 8):
+    def __init__(self, size: int = 8, budget: int = None):
         self.size = size
-        self.entries = []   # (key, weakref(angles), version, plan tensor)
+        self.budget = _plan_budget() if budget is None else budget
+        self.entries = []   # (key, weakref(angles), version, plan entry, bytes)
+
+    @staticmethod
+    def _bytes(entry) -> int:
+        plan = entry[0] if isinstance(entry, tuple) else entry
+        return int(plan.numel()) * int(plan.element_size())
 
     def get(self, key, angles, build):
         import weakref
-        for i, (k, ref, ver, plan) in enumerate(self.entries):
+        for i, (k, ref, ver, plan, _) in enumerate(self.entries):
             if k == key and ref() is angles and ver == angles._version:
                 self.entries.insert(0, self.entries.pop(i))
                 return plan
         plan = build()
-        self.entries.insert(0, (key, weakref.ref(angles), angles._version, plan))
+        self.entries.insert(0, (key, weakref.ref(angles), angles._version, plan, self._bytes(plan)))
         del self.entries[self.size:]
+        while len(self.entries) > 1 and self.nbytes() > self.budget:
+            self.entries.pop()
         return plan
+
+    def nbytes(self) -> int:
+        return sum(e[4] for e in self.entries)
 
     def clear(self):
         self.entries.clear()
