@@ -142,6 +142,71 @@ def test_spiral_full_geometry_subset_of_views(golden3d, oracle_mod):
     assert e <= 1e-5 and eo <= 5e-5
 
 
+def _dot_and_fd(label, fwd, adj, x, ang_all, ang_fd, nvox=64, seed=0):
+    """Dot test of (fwd, adj) on all of `ang_all` (FP64 accumulation) and
+    central finite differences of ||A x - b||^2 on `ang_fd` at `nvox` voxels
+    that the views see (the loss is quadratic and a voxel changes only the
+    cells its rays cross, so FD carries no truncation error)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ax = fwd(x, ang_all)
+    y = torch.rand(ax.shape, device="cuda", generator=g)
+    aty = adj(y, ang_all)
+    lhs = float((ax.double() * y.double()).sum())
+    rhs = float((x.double() * aty.double()).sum())
+    dot = abs(lhs - rhs) / abs(lhs)
+    del ax, y, aty
+    b = fwd(x, ang_fd) * 0.9
+    base = x * 1.05
+    r = fwd(base, ang_fd) - b
+    grad = 2.0 * adj(r, ang_fd)
+    flat = grad.view(-1)
+    cand = torch.nonzero(flat.abs() > 1e-3 * float(flat.abs().max())).view(-1)
+    pick = cand[torch.randperm(cand.numel(), device="cuda", generator=g)[:nvox]]
+    h = 1e-2 * float(x.abs().max())
+    fd, ag = [], []
+    for k in pick.tolist():
+        e = torch.zeros_like(base).view(-1)
+        e[k] = h
+        e = e.view_as(base)
+        lp = ((fwd(base + e, ang_fd) - b).double() ** 2).sum()
+        lm = ((fwd(base - e, ang_fd) - b).double() ** 2).sum()
+        fd.append(float((lp - lm) / (2 * h)))
+        ag.append(float(flat[k]))
+    err = rel_l2(np.array(ag), np.array(fd))
+    print(f"{label}: dot rel {dot:.2e} ({ang_all.numel()} views), FD vs A^T at {len(fd)} voxels {err:.2e}")
+    assert dot <= 1e-6
+    assert err <= 1e-3
+
+
+def test_cone_beam_configuration_dot_and_fd():
+    """2 x 256^3, 512 x 384 detector, SID 500 / SDD 1000: the dot test on all
+    360 views, finite differences on 36 of them."""
+    from pridediff_gb300 import radontorch as RT
+    opt, ang_np = cases3d.cone_256cube()
+    ot = torch.tensor(opt)
+    x = torch.from_numpy(np.stack([cases3d.ellipsoids(256, 256, 256, 12, s) for s in (4, 5)])[:, None]).cuda()
+    ang = torch.from_numpy(ang_np).cuda()
+    _dot_and_fd("cone-flat 2 x 256^3", lambda v, a: RT.ProjConeFlatDis3d(v, ot, a),
+                lambda w, a: RT.ProjTransConeFlatDis3d(w, ot, a), x, ang, ang[::10].contiguous(), seed=4)
+
+
+def test_spiral_configuration_dot_and_fd():
+    """2 x 512 x 512 x 128, 64 x 736 arc detector, pitch 1: the dot test on
+    the 1152 views of the middle turn, finite differences on 24 of them."""
+    from pridediff_gb300 import radontorch as RT
+    opt, ang_np, sp_np = cases3d.spiral_512x128()
+    ot = torch.tensor(opt)
+    turn = slice(1152, 2304)
+    ang = torch.from_numpy(ang_np[turn].copy()).cuda()
+    sp = torch.from_numpy(sp_np[:, turn].copy()).cuda()
+    sel = torch.arange(0, 1152, 48, device="cuda")
+    sps = {ang.numel(): sp, sel.numel(): sp[:, sel].contiguous()}
+    x = torch.from_numpy(np.stack([cases3d.ellipsoids(128, 512, 512, 12, s, 0.04) for s in (6, 7)])[:, None]).cuda()
+    _dot_and_fd("spiral 2 x 512x512x128", lambda v, a: RT.ProjSpiralDis3d(v, ot, a, sps[a.numel()]),
+                lambda w, a: RT.ProjTransSpiralDis3d(w, ot, a, sps[a.numel()]), x, ang, ang[sel].contiguous(),
+                seed=6)
+
+
 def test_projector3d_autograd_gradient_is_the_adjoint():
     import pridediff_gb300 as P
     proj = P.projector3d((32, 28, 20), (48, 24), 1.0, 1.0, 300.0, 600.0, scan_type="flat").cuda()
