@@ -153,6 +153,42 @@ def test_config3_uneven_24_instances_50_captured_steps():
     assert rel_l2(ub.pack(parts).cpu().numpy(), xc.cpu().numpy()) <= 1e-5
 
 
+def test_dc_step_size_against_power_iteration():
+    """lambda_max(A^T A) of the 512^2 fan-flat geometry (720 views, 736
+    detectors) by power iteration, and what it means for the batched
+    configuration's step x <- x - eta A^T (A x - y): with eta below
+    2 / lambda_max the residual falls every step, with eta = 1e-3 (the
+    configuration's value) it grows."""
+    import pridediff_gb300 as P
+    proj = P.projector2d(512, 736, 0.66, 1.2858, 595.0, 1085.6, scan_type="flat").cuda()
+    ang = torch.arange(720, dtype=torch.float32, device="cuda") * (2 * np.pi / 720)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    v = torch.rand((1, 1, 512, 512), device="cuda", generator=g)
+    lam = 0.0
+    for _ in range(30):
+        w = proj.projection_t(proj.projection(v, ang), ang)
+        lam = float((w.double() * v.double()).sum() / (v.double() ** 2).sum())
+        v = w / w.norm()
+    print(f"lambda_max(A^T A) ~ {lam:.4e} (512^2, 720 views, 736 dets)")
+    assert 1e4 < lam < 1e6
+    x_true = torch.rand((1, 1, 512, 512), device="cuda", generator=g) * 0.04
+    y = proj.projection(x_true, ang)
+
+    def residuals(eta, steps):
+        x = torch.zeros_like(x_true)
+        out = []
+        for _ in range(steps):
+            r = proj.projection(x, ang) - y
+            out.append(float(r.double().norm()))
+            x = x - eta * proj.projection_t(r, ang)
+        return out
+
+    stable = residuals(1.0 / lam, 6)
+    assert all(b < a for a, b in zip(stable, stable[1:]))
+    unstable = residuals(1e-3, 6)
+    assert unstable[-1] > 10 * unstable[0]
+
+
 def test_uneven_24_instance_configuration_matches_reference_cpu(oracle_mod):
     """Every instance of the 24-instance uneven configuration (image sizes
     {256,384,512}^2, views {360,576,720}, detectors {368,512,736}; the draw
