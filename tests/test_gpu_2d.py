@@ -160,7 +160,7 @@ def test_autograd_gradient_matches_adjoint_and_fd():
     assert rel_l2(x0.grad.cpu().numpy(), gref.cpu().numpy()) == 0.0
     # central finite differences at 64 pixels (quadratic loss: no truncation error)
     idx = rng.choice(512 * 512, 64, replace=False)
-    h = 1e-2 * float(x0.max())
+    h = 1e-2 * float(x0.detach().max())
     base = x0.detach().clone()
     fd = []
     for k in idx:
