@@ -18,6 +18,7 @@ import pytest
 import torch
 
 import cases3d
+from cases3d import spiral_source
 from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -140,6 +141,68 @@ def test_spiral_full_geometry_subset_of_views(golden3d, oracle_mod):
     eo = rel_l2(bt, oracle_mod.run3d("spiral", "proj_t", y, ang[sel], opt, source_pos=sps, prec="f", nthreads=8))
     print(f"spiral 512x512x128 proj_t, 6 views: rel-L2 vs reference CUDA {e:.2e}, vs FP32 oracle {eo:.2e}")
     assert e <= 1e-5 and eo <= 5e-5
+
+
+def _fuzz3d(n=12, seed=77):
+    """Seeded random small 3-D geometries: volume and detector sizes, voxel
+    aspect, SID / SDD, shifts, detector cells of 0.8 to 2.5 voxels at the
+    isocentre (narrower cells make the comparison with the FP32 oracle, whose
+    trigonometry rounds differently from the device's, ill-conditioned),
+    random view angles, for spirals a random pitch and source table."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        geom = ("cone_flat", "cone_arc", "spiral")[i % 3]
+        W, H = (int(v) for v in rng.integers(8, 49, 2))
+        D = int(rng.integers(4, 25))
+        px, py, pz = (float(v) for v in rng.uniform(0.6, 1.5, 3))
+        sid = float(rng.uniform(250.0, 600.0))
+        sdd = sid * float(rng.uniform(1.5, 2.2))
+        mag = sdd / sid
+        cw = max(px, py) * float(rng.uniform(0.8, 2.5))          # column width at the isocentre
+        rw = pz * float(rng.uniform(0.8, 2.5))
+        C = int(min(300, np.hypot(W * px, H * py) * 1.2 / cw) + 2)
+        R = int(min(32, D * pz * 1.3 / rw) + 2) if geom != "spiral" else int(rng.integers(4, 12))
+        col = cw * mag if geom == "cone_flat" else cw / sid
+        row = rw * mag
+        V = int(rng.integers(2, 13))
+        ang = rng.uniform(0, 2 * np.pi, V).astype(np.float32)
+        sh = rng.uniform(-0.4, 0.4, 5) * np.array([px, py, pz, cw, rw])
+        if geom != "cone_flat":
+            sh[3] /= sid                                         # arc column shift is an angle
+        if geom == "spiral":
+            opt = np.array([W, H, D, C, R, px, py, pz, col, row, sid, sdd, sh[0], sh[1], sh[3], sh[4]], np.float32)
+            pitch = float(rng.uniform(0.2, 1.5))
+            sp = spiral_source(V, pitch, -pitch * (V - 1) / 2, float(rng.uniform(-1, 1)),
+                               float(rng.uniform(-1e-3, 1e-3)), float(rng.uniform(-0.2, 0.2)))
+        else:
+            opt = np.array([W, H, D, C, R, px, py, pz, col, row, sid, sdd] + list(sh), np.float32)
+            sp = None
+        out.append((geom, opt, ang, sp))
+    return out
+
+
+FUZZ3 = _fuzz3d()
+
+
+@pytest.mark.parametrize("case", range(len(FUZZ3)))
+def test_random_3d_geometries_match_oracle_and_are_adjoint(oracle_mod, case):
+    """All 6 operators of each seeded random 3-D geometry against the FP32
+    oracle (5e-5, as for the fixed small cases), and the dot test of each
+    operator pair."""
+    geom, opt, ang, sp = FUZZ3[case]
+    x, y = cases3d.inputs((geom, opt, ang, sp), batch=2, seed=900 + case)
+    outs = {}
+    for op in cases3d.OPS:
+        inp = x if op in cases3d.IMAGE_IN else y
+        out = run(geom, op, inp, ang, opt, sp)
+        ref = oracle_mod.run3d(geom, op, inp, ang, opt, source_pos=sp, prec="f", nthreads=8)
+        e = rel_l2(out, ref) if np.any(ref) else float(np.abs(out).max())
+        assert e <= 5e-5, (case, geom, opt.tolist(), op, e)
+        outs[op] = out.astype(np.float64)
+    for fwd, adj in (("proj", "proj_t"), ("bproj_t", "bproj"), ("bproj_tw", "bproj_w")):
+        lhs, rhs = float((outs[fwd] * y).sum()), float((x * outs[adj]).sum())
+        assert abs(lhs - rhs) <= 1e-6 * max(abs(lhs), 1e-30), (case, fwd, lhs, rhs)
 
 
 def _dot_and_fd(label, fwd, adj, x, ang_all, ang_fd, nvox=64, seed=0):
