@@ -399,8 +399,9 @@ k_trange(dd_geom2d g, int V, const DdView2 *__restrict__ views, const float *__r
 }
 
 // Single-geometry adjoint launch: grid (tiles x * image groups, tiles y).
+// Fan beams: 4 CTAs per SM (64 registers), as the persistent adjoint.
 template <int GEOM, int OPK>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, GEOM == DD_GEOM_PARA ? 1 : 4)
 k_adj(dd_geom2d g, int B, int V, int nl, const float *__restrict__ angles,
       const DdView2 *__restrict__ views, const float *__restrict__ dp,
       const DdLine *__restrict__ lines, const DdLine *__restrict__ dlines, const unsigned char *__restrict__ amap,

@@ -606,6 +606,9 @@ constexpr int kStage = 256;
 // while view v is computed (part of the map comes from HBM).
 constexpr int kAdjBufs = 3;
 
+static_assert((kAdjBufs * kMapBlkBytes + kAdjBufs * kBI * kStage * 8) % 16 == 0,
+              "the fan adjoint's per-buffer copy descriptors must be 16-byte aligned");
+
 // Shared-memory layout of the adjoint kernel (bytes).  Parallel beam: line
 // records (and detector-side records); fan beams: adjoint-map rows, detector
 // table slices and per-line scales.
@@ -622,7 +625,7 @@ __host__ __device__ inline AdjSmem adj_smem(int geom) {
         s.rec = s.drec = s.kd = 0;
         s.map = o; o += kAdjBufs * kMapBlkBytes;
         s.stage = o; o += kAdjBufs * kBI * kStage * (int)sizeof(float2);
-        s.krange = o; o += 4 * kAdjBufs * (int)sizeof(int);
+        s.krange = o; o += 4 * kAdjBufs * (int)sizeof(int);   // 16-byte aligned: read as int4
         s.bar = o; o += kAdjBufs * (int)sizeof(uint64_t);
         s.total = (o + 127) & ~127;
         return s;
@@ -1032,17 +1035,21 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
         issue(0, 0, d0);
         if (V > 1) issue(1, 1, d1);
     }
-    int2 tr_next = (V > 2) ? it.trange[(size_t)2 * ntiles + tile] : make_int2(0, 0);   // view v + 2
+    // only the warps that issue a view's copies (warp 0: the map block, warps
+    // 1 .. nb: the detector slices) need its descriptor
+    const bool issuing = warp <= nb;
+    int2 tr_next = (V > 2 && issuing) ? it.trange[(size_t)2 * ntiles + tile] : make_int2(0, 0);   // view v + 2
     int vstop = V;   // first view not waited for (the copies of vstop may be in flight)
-    for (int v = 0; v < V; v++) {
-        const int buf = v % kAdjBufs;
+    int buf = 0, buf2 = 2 % kAdjBufs;   // buffers of views v and v + 2
+    for (int v = 0; v < V; v++, buf = (buf + 1 == kAdjBufs) ? 0 : buf + 1,
+                                buf2 = (buf2 + 1 == kAdjBufs) ? 0 : buf2 + 1) {
         const bool more = v + 2 < V;
         Cp dn;
-        if (more) {
+        if (more && issuing) {
             dn = desc(tr_next);
             // the phase of view v - 1 on this barrier was waited for before the
             // previous barrier, so it can be armed for view v + 2 now
-            if (tid == 0) arm((v + 2) % kAdjBufs, dn);
+            if (tid == 0) arm(buf2, dn);
         }
         if (!dd_mbar_wait(&bar[buf], ph.parity(buf))) abort_flag = 1;
         ph.flip(buf);
@@ -1055,12 +1062,12 @@ __device__ bool adj_tile_map(const dd_geom2d &g, const AdjItem &it, unsigned cha
             break;
         }
         // so the copies of view v + 2 go into the buffer of view v - 1
-        if (more) {
-            issue(v + 2, (v + 2) % kAdjBufs, dn);
+        if (more && issuing) {
+            issue(v + 2, buf2, dn);
             if (v + 3 < V) tr_next = it.trange[(size_t)(v + 3) * ntiles + tile];
         }
-        const int kb = krange[4 * buf], kn = krange[4 * buf + 1], elo = krange[4 * buf + 2];
-        const int xb = krange[4 * buf + 3];
+        const int4 kr = reinterpret_cast<const int4 *>(krange)[buf];   // one 16-byte load
+        const int kb = kr.x, kn = kr.y, elo = kr.z, xb = kr.w;
         const int2 *mp = reinterpret_cast<const int2 *>(mapb + (size_t)buf * kMapBlkBytes);
         const float *alb = reinterpret_cast<const float *>(mp + kTile * kMapE);   // line scales
         const float2 *sb = stage + (size_t)buf * kBI * kStage;
