@@ -41,12 +41,25 @@ struct BatchLayout {
     size_t desc, fitems, aitems, plans, total;        // plan buffer
     size_t w_tabs, w_dtab, w_resid, w_counter, w_status, w_total;   // workspace
     int nfwd, nadj, Dmax, rsmax;
+    int fi;   // slices per forward item (fwd_item_slices)
     std::vector<BatchInst> inst;
 };
+
+// Slices per persistent forward item: 2 where no instance has more than 2
+// slices (after instances with one geometry are merged, the usual uneven
+// batch), so that the forward kernel holds half the line tables and runs 6
+// CTAs per SM instead of 5 (24 uneven instances: 6.51 -> 6.16 ms); kBI
+// otherwise, where 4 slices share each locate.
+static int fwd_item_slices(const dd_instance2d *in, int n) {
+    int mb = 0;
+    for (int i = 0; i < n; i++) mb = std::max(mb, in[i].batch);
+    return mb <= 2 ? 2 : kBI;
+}
 
 static BatchLayout batch_layout(int scan, const dd_instance2d *in, int n, int bi) {
     BatchLayout L;
     L.inst.resize(n);
+    L.fi = fwd_item_slices(in, n);
     long long img = 0, sino = 0, tabs = 0, dtab = 0;
     size_t plans = 0;
     L.nfwd = L.nadj = 0;
@@ -83,7 +96,7 @@ static BatchLayout batch_layout(int scan, const dd_instance2d *in, int n, int bi
         d.dtab_off = dtab;
         dtab += ((long long)d.batch * d.V * rs_entries(D) + 1) & ~1LL;
         const int groups = (d.batch + bi - 1) / bi;
-        L.nfwd += d.V * groups;
+        L.nfwd += d.V * ((d.batch + L.fi - 1) / L.fi);
         L.nadj += ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile) * groups;
         L.Dmax = std::max(L.Dmax, D);
         L.rsmax = std::max(L.rsmax, rs_entries(std::max(W, H)));
@@ -186,10 +199,13 @@ __device__ __forceinline__ int next_item_cluster(int *counter) {
     return i;
 }
 
-// Resident CTAs per SM the persistent forward is compiled for (48 registers
-// per thread up to 4 passes; on 24 uneven one-slice instances 5 CTAs per SM
-// ran the forward in 8.13 ms, 6 in 8.20 ms).
-__host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <= 4 ? 5 : 3; }
+// Resident CTAs per SM the persistent forward is compiled for: items of 4
+// slices, 48 registers per thread up to 4 passes (on 24 uneven one-slice
+// instances 5 CTAs per SM ran the forward in 8.13 ms, 6 in 8.20 ms); items
+// of 2 slices, 40 registers and 6 CTAs.
+__host__ __device__ constexpr int fwd_items_min_ctas(int npass, int bi) {
+    return npass <= 4 ? (bi <= 2 ? 6 : 5) : 3;
+}
 
 // CTAs per persistent-forward cluster.  Batches of many short items leave
 // little tail to split: on 24 uneven one-slice instances, clusters of 2 (an
@@ -202,14 +218,14 @@ __host__ __device__ constexpr int fwd_items_min_ctas(int npass) { return npass <
 // autotuner finds 2 faster for the batch at hand.
 constexpr int kFwdItemsCluster = 1;
 
-template <int GEOM, int NPASS, int CL>
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS))
+template <int GEOM, int NPASS, int CL, int BI>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(kThreads, fwd_items_min_ctas(NPASS, BI))
 k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__ items, int nitems,
             const char *__restrict__ plan, size_t plans_off, const float2 *__restrict__ tabs,
             float *__restrict__ out, const float *__restrict__ sub, int Dmax, int rsmax,
             int *__restrict__ counter, int *__restrict__ status) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, kBI, CL);
+    const FwdSmem L = fwd_smem(GEOM, Dmax, rsmax, BI, CL);
     init_bars(reinterpret_cast<uint64_t *>(smem + L.bar));
     // the item and its geometry live in shared memory: read where used, they
     // hold no registers across the line loop (the plain forward reads them
@@ -245,7 +261,7 @@ k_fwd_items(int op, const BatchInst *__restrict__ desc, const int4 *__restrict__
             s_g = d.g;
         }
         __syncthreads();   // every thread passed the cluster barrier above before s_it changes
-        if (!fwd_view<GEOM, 0, NPASS, kBI, kWarps, CL>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
+        if (!fwd_view<GEOM, 0, NPASS, BI, kWarps, CL>(s_g, op, s_it, smem, Dmax, rsmax, ph)) {
             if (threadIdx.x == 0) dd_report_timeout(status);
             break;
         }
@@ -371,14 +387,14 @@ static int cluster_grid_of(const dd_tune2d *t, int nitems, K kern, int smem, int
     return clusters * cl;
 }
 
-template <int GEOM, int CL>
+template <int GEOM, int CL, int BI>
 static auto fwd_items_kernel(int Dmax) {
-    auto kern = k_fwd_items<GEOM, 8, CL>;
+    auto kern = k_fwd_items<GEOM, 8, CL, BI>;
     switch (npass_class(Dmax)) {
-    case 1: kern = k_fwd_items<GEOM, 1, CL>; break;
-    case 2: kern = k_fwd_items<GEOM, 2, CL>; break;
-    case 3: kern = k_fwd_items<GEOM, 3, CL>; break;
-    case 4: kern = k_fwd_items<GEOM, 4, CL>; break;
+    case 1: kern = k_fwd_items<GEOM, 1, CL, BI>; break;
+    case 2: kern = k_fwd_items<GEOM, 2, CL, BI>; break;
+    case 3: kern = k_fwd_items<GEOM, 3, CL, BI>; break;
+    case 4: kern = k_fwd_items<GEOM, 4, CL, BI>; break;
     default: break;
     }
     return kern;
@@ -389,9 +405,11 @@ static int launch_fwd_items(int op, const BatchLayout &L, const char *planb, con
                             float *out, const float *sub, int *counter, int *status, const dd_tune2d *tune,
                             cudaStream_t st) {
     int cl = (tune && tune->items_cluster == 2) ? 2 : kFwdItemsCluster;
-    if (cl == 2 && fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, 2).total > max_smem_optin()) cl = 1;
-    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, kBI, cl);
-    auto kern = (cl == 2) ? fwd_items_kernel<GEOM, 2>(L.Dmax) : fwd_items_kernel<GEOM, 1>(L.Dmax);
+    if (cl == 2 && fwd_smem(GEOM, L.Dmax, L.rsmax, L.fi, 2).total > max_smem_optin()) cl = 1;
+    const FwdSmem S = fwd_smem(GEOM, L.Dmax, L.rsmax, L.fi, cl);
+    auto kern = (L.fi == 2)
+        ? ((cl == 2) ? fwd_items_kernel<GEOM, 2, 2>(L.Dmax) : fwd_items_kernel<GEOM, 1, 2>(L.Dmax))
+        : ((cl == 2) ? fwd_items_kernel<GEOM, 2, kBI>(L.Dmax) : fwd_items_kernel<GEOM, 1, kBI>(L.Dmax));
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S.total) != cudaSuccess)
         return DD_ERR_LAUNCH;
     const int grid = cluster_grid_of(tune, L.nfwd, kern, S.total, cl);
@@ -507,10 +525,13 @@ extern "C" int dd2d_batch_plan(int scan, const dd_instance2d *inst, int n, const
     for (int i = 0; i < n; i++) {
         const BatchInst &d = L.inst[i];
         const int W = d.g.width, H = d.g.height, D = d.g.num_det;
-        for (int b0 = 0; b0 < d.batch; b0 += kBI) {
-            const int nb = std::min(kBI, d.batch - b0);
+        for (int b0 = 0; b0 < d.batch; b0 += L.fi) {
+            const int nb = std::min(L.fi, d.batch - b0);
             for (int v = 0; v < d.V; v++)
                 fw.push_back({make_int4(i, v, b0, nb), (long long)std::max(W, H) * (D + 1) * nb});
+        }
+        for (int b0 = 0; b0 < d.batch; b0 += kBI) {
+            const int nb = std::min(kBI, d.batch - b0);
             for (int ty = 0; ty < (H + kTile - 1) / kTile; ty++)
                 for (int tx = 0; tx < (W + kTile - 1) / kTile; tx++)
                     aw.push_back({make_int4(i, tx | (ty << 16), b0, nb), (long long)d.V * nb});
