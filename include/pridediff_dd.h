@@ -144,7 +144,7 @@ typedef struct dd_tune2d {
     int ctas_per_sm;    /* persistent CTAs per SM (0 = as many as fit; capped at that) */
     int lpt_order;      /* items longest-first (1) or in instance order (0) */
     /* single-geometry forward (dd2d_apply_planned_tuned): */
-    int fwd_slices;     /* slices per CTA: 4 (default) or 2 */
+    int fwd_slices;     /* slices per CTA: 4 (default) or 1 */
     int fwd_cluster;    /* CTAs sharing a view's walked lines, a cluster: 2 (default) or 1 */
     /* persistent forward: */
     int items_cluster;  /* CTAs sharing an item's walked lines: 1 (default) or 2 */

@@ -115,7 +115,7 @@ def recorded(key: str, path: Optional[str] = None) -> Dict[str, float]:
 BATCH_CANDIDATES = [{"ctas_per_sm": c, "lpt_order": o, "items_cluster": k}
                     for c in (0, 2, 4) for o in (1, 0) for k in (1, 2)]
 # single-geometry forward: slices per CTA x CTAs per view's cluster
-FORWARD2D_CANDIDATES = [{"fwd_slices": b, "fwd_cluster": c} for b in (4, 2) for c in (2, 1)]
+FORWARD2D_CANDIDATES = [{"fwd_slices": b, "fwd_cluster": c} for b in (4, 1) for c in (2, 1)]
 
 
 def enabled() -> bool:

@@ -1,6 +1,6 @@
 """Edge sizes of the 2-D operators against the FP32 oracle: a single pixel, a
 single view, the largest detector (1984 bins, the widest pass class), lines
-of 4096 pixels (the forward then stages 2 images per CTA instead of 4),
+of 4096 pixels (the forward then stages 1 image per CTA instead of 4),
 batches that are not a multiple of the 4 images a CTA takes."""
 import numpy as np
 import pytest
