@@ -336,7 +336,8 @@ int dd_profile_enable(int on);
  * synchronises on the recorded events. */
 int dd_profile_read(int kind, double *total_ms, int *count);
 const char *dd_status_string(int status);
-/* Library version and build target, e.g. "pridediff_dd 0.1 sm_103a". */
+/* Library version and build target, e.g. "pridediff_dd 0.2 sm_103a"; part of
+ * the autotuner's cache key, so choices recorded by another version are not reused. */
 const char *dd_version(void);
 
 #ifdef __cplusplus

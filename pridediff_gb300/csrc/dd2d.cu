@@ -904,7 +904,7 @@ extern "C" const char *dd_status_string(int status) {
     }
 }
 
-extern "C" const char *dd_version(void) { return "pridediff_dd 0.1 sm_103a"; }
+extern "C" const char *dd_version(void) { return "pridediff_dd 0.2 sm_103a"; }
 
 extern "C" unsigned long long dd_launch_count(void) { return g_launches; }
 
