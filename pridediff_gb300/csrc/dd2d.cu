@@ -90,15 +90,38 @@ __global__ void k_tab_rows(const float *__restrict__ img, int B, int H, int W,
 }
 
 // Column lines (y-branch): line = image column, walked from the bottom row.
-// One thread per (image, column): coalesced reads along a row.
-__global__ void k_tab_cols(const float *__restrict__ img, int B, int H, int W,
-                           float2 *__restrict__ tab) {
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= B * W) return;
-    const int b = idx / W, col = idx - b * W;
-    const float *im = img + (size_t)b * H * W;
-    float2 *t = tab + (size_t)idx * rs_entries(H);
-    col_prefix_table(im, H, W, col, t);
+// A block takes 32 columns of one image (lanes: coalesced reads along a row)
+// and splits the rows into kColChunks chunks (warps): each warp sums its
+// chunk in double-float arithmetic, the chunk totals are added in order, and
+// each warp then writes its rows' prefixes from its chunk's start -- 8 times
+// the threads of one walk per column.
+constexpr int kColChunks = 8;
+__global__ void __launch_bounds__(32 * kColChunks)
+k_tab_cols(const float *__restrict__ img, int B, int H, int W, float2 *__restrict__ tab) {
+    const int c = threadIdx.x & 31, k = threadIdx.x >> 5;
+    const int ncb = (W + 31) / 32;
+    const int b = blockIdx.x / ncb, col = (blockIdx.x - b * ncb) * 32 + c;
+    const int per = (H + kColChunks - 1) / kColChunks;
+    const int i0 = min(H, k * per), i1 = min(H, i0 + per);
+    const bool ok = b < B && col < W;
+    const float *__restrict__ im = img + (size_t)b * H * W + col;
+    __shared__ float tot_hi[kColChunks][32], tot_lo[kColChunks][32];
+    DdF run = {0.0f, 0.0f};
+    if (ok)
+        for (int i = i0; i < i1; i++) run = df_add(run, DdF{__ldg(im + (size_t)(H - 1 - i) * W), 0.0f});
+    tot_hi[k][c] = run.hi;
+    tot_lo[k][c] = run.lo;
+    __syncthreads();
+    if (!ok) return;
+    run = {0.0f, 0.0f};
+    for (int q = 0; q < k; q++) run = df_add(run, DdF{tot_hi[q][c], tot_lo[q][c]});
+    float2 *__restrict__ t = tab + ((size_t)b * W + col) * rs_entries(H);
+    for (int i = i0; i < i1; i++) {
+        const float x = __ldg(im + (size_t)(H - 1 - i) * W);
+        t[i] = make_float2(run.hi, x);
+        run = df_add(run, DdF{x, 0.0f});
+    }
+    if (i0 < H && i1 == H) t[H] = make_float2(run.hi, 0.0f);
 }
 
 // Detector tables for the adjoint: per (image, view) G_k and g_k over the
@@ -669,7 +692,7 @@ int launch_image_tables(const dd_geom2d *g, const float *in, int B, float2 *tx, 
     const int nw = B * H;
     ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
     k_tab_rows<<<(nw * 32 + 255) / 256, 256, 0, st>>>(in, B, H, W, tx);
-    k_tab_cols<<<(B * W + 127) / 128, 128, 0, st>>>(in, B, H, W, ty);
+    k_tab_cols<<<B * ((W + 31) / 32), 32 * kColChunks, 0, st>>>(in, B, H, W, ty);
     prof_end(pr, st);
     g_launches += 2;
     return launch_status();

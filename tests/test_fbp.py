@@ -47,9 +47,16 @@ def _correlate(x, w, taps):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_taps_and_weights_match_reference(fbp_golden, name):
+    """Filter taps and cosine weights equal to deeprecon's (fixtures made on an
+    x86-64 host).  The weights come from torch's cos / atan: another host's
+    math library may round a few of them one ulp apart."""
+    import platform
     prj = _projector(fbp_golden, name)
     assert np.array_equal(prj.filter.detach().numpy().reshape(-1), fbp_golden[f"{name}/filter"])
-    assert np.array_equal(prj.weight.detach().numpy(), fbp_golden[f"{name}/weight"])
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert np.array_equal(prj.weight.detach().numpy(), fbp_golden[f"{name}/weight"])
+    else:
+        np.testing.assert_array_max_ulp(prj.weight.detach().numpy(), fbp_golden[f"{name}/weight"], maxulp=1)
     for other in ("ramp", "sheeplogan"):
         assert np.array_equal(prj.filter_generate(other).numpy().reshape(-1), fbp_golden[f"{name}/taps_{other}"])
 
