@@ -134,16 +134,37 @@ __global__ void k_tab_rows_b(const BatchInst *__restrict__ desc, const float *__
     });
 }
 
-__global__ void k_tab_cols_b(const BatchInst *__restrict__ desc, const float *__restrict__ img,
-                             float2 *__restrict__ tabs) {
+// Column tables as the single-geometry k_tab_cols builds them: a block takes
+// 32 of an instance's (image, column) lines, its 8 warps a chunk of rows each.
+__global__ void __launch_bounds__(256) k_tab_cols_b(const BatchInst *__restrict__ desc,
+                                                    const float *__restrict__ img, float2 *__restrict__ tabs) {
+    constexpr int kChunks = 8;
     const BatchInst &d = desc[blockIdx.y];
     const int W = d.g.width, H = d.g.height;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= d.batch * W) return;
-    const int b = idx / W, col = idx - b * W;
-    const float *im = img + d.img_off + (size_t)b * H * W;
-    float2 *t = tabs + d.taby_off + (size_t)idx * rs_entries(H);
-    col_prefix_table(im, H, W, col, t);
+    const int c = threadIdx.x & 31, k = threadIdx.x >> 5;
+    const int idx = blockIdx.x * 32 + c;
+    const bool ok = idx < d.batch * W;
+    const int b = ok ? idx / W : 0, col = ok ? idx - b * W : 0;
+    const int per = (H + kChunks - 1) / kChunks;
+    const int i0 = min(H, k * per), i1 = min(H, i0 + per);
+    const float *__restrict__ im = img + d.img_off + (size_t)b * H * W + col;
+    __shared__ float tot_hi[kChunks][32], tot_lo[kChunks][32];
+    DdF run = {0.0f, 0.0f};
+    if (ok)
+        for (int i = i0; i < i1; i++) run = df_add(run, DdF{__ldg(im + (size_t)(H - 1 - i) * W), 0.0f});
+    tot_hi[k][c] = run.hi;
+    tot_lo[k][c] = run.lo;
+    __syncthreads();
+    if (!ok) return;
+    run = {0.0f, 0.0f};
+    for (int q = 0; q < k; q++) run = df_add(run, DdF{tot_hi[q][c], tot_lo[q][c]});
+    float2 *__restrict__ t = tabs + d.taby_off + (size_t)idx * rs_entries(H);
+    for (int i = i0; i < i1; i++) {
+        const float x = __ldg(im + (size_t)(H - 1 - i) * W);
+        t[i] = make_float2(run.hi, x);
+        run = df_add(run, DdF{x, 0.0f});
+    }
+    if (i0 < H && i1 == H) t[H] = make_float2(run.hi, 0.0f);
 }
 
 __global__ void k_dettab_b(int geom, int mode, const BatchInst *__restrict__ desc,
@@ -456,7 +477,7 @@ static int batch_forward(int scan, int op, const BatchLayout &L, const char *pla
     const int n = (int)L.inst.size();
     ProfRec *pr = prof_begin(DD_KERNEL_TABLES, st);
     k_tab_rows_b<<<dim3((maxrows * 32 + 255) / 256, n), 256, 0, st>>>(desc, in, tabs);
-    k_tab_cols_b<<<dim3((maxcols + 127) / 128, n), 128, 0, st>>>(desc, in, tabs);
+    k_tab_cols_b<<<dim3((maxcols + 31) / 32, n), 256, 0, st>>>(desc, in, tabs);
     prof_end(pr, st);
     count_launches(2);
     if (cudaMemsetAsync(counter, 0, 2 * sizeof(int), st) != cudaSuccess) return DD_ERR_LAUNCH;

@@ -213,32 +213,6 @@ __device__ __forceinline__ float fan_fbp_weight(float sx, float sy, float px, fl
     return t * t;
 }
 
-// One thread: the prefix table of image column `col` walked from the bottom
-// row (entries (S_i, x_i), S in double-float arithmetic rounded once, entry H
-// = (S_H, 0)).  Rows are loaded 8 ahead of the dependent sums; the order of
-// the additions is the plain sequential one.
-__device__ __forceinline__ void col_prefix_table(const float *__restrict__ im, int H, int W, int col,
-                                                 float2 *__restrict__ t) {
-    DdF run = {0.0f, 0.0f};
-    int i = 0;
-    for (; i + 8 <= H; i += 8) {
-        float xs[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) xs[u] = __ldg(im + (size_t)(H - 1 - (i + u)) * W + col);
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            t[i + u] = make_float2(run.hi, xs[u]);
-            run = df_add(run, DdF{xs[u], 0.0f});
-        }
-    }
-    for (; i < H; i++) {
-        const float x = __ldg(im + (size_t)(H - 1 - i) * W + col);
-        t[i] = make_float2(run.hi, x);
-        run = df_add(run, DdF{x, 0.0f});
-    }
-    t[H] = make_float2(run.hi, 0.0f);
-}
-
 struct Loc {
     int p, j;
     float dl, r;
